@@ -1,0 +1,134 @@
+/*
+ * libFourierConvolutionCUDA -- GB300 (sm_103a) drop-in for the native library behind
+ * fiji/SPIM_Registration's multiview Bayesian deconvolution.
+ *
+ * Part 1 is the C ABI the reference binds through JNA (method name == symbol name); the
+ * prototypes follow the Java interfaces they replace.  Part 2 adds status-returning and
+ * whole-iteration entry points for a Java loop that keeps the views resident on the GPU.
+ *
+ * Conventions: all images are float32, x fastest (imglib2 ArrayImg layout).  The JNA calls
+ * pass dimensions reversed, {z, y, x}, as MVDeconFFTThreads.getCUDACoordinates does
+ * (spim/process/fusion/deconvolution/MVDeconFFTThreads.java:157-165); the mvd_* calls take
+ * {x, y, z}.  Kernels have odd sizes with their centre at size/2.
+ */
+#ifndef MVDECON_H
+#define MVDECON_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ===================== Part 1: the reference's JNA interface ===================== */
+
+/* spim/process/cuda/CUDAStandardFunctions.java:36-44 */
+int getCUDAcomputeCapabilityMinorVersion(int devCUDA);
+int getCUDAcomputeCapabilityMajorVersion(int devCUDA);
+/* -1 if the driver failed (CUDAStandardFunctions.java:38-41), else the device count */
+int getNumDevicesCUDA(void);
+/* writes a NUL-terminated name into a 256-byte buffer (CUDATools.java:76) */
+void getNameDeviceCUDA(int devCUDA, char* name);
+long long getMemDeviceCUDA(int devCUDA);
+long long getFreeMemDeviceCUDA(int devCUDA);
+
+/* spim/process/cuda/CUDAFourierConvolution.java:30 -- declared by the reference, never called
+ * by it; returns NULL and records an error (mvd_last_error). */
+float* convolution3DfftCUDA(float* im, int* imDim, float* kernel, int* kernelDim, int devCUDA);
+
+/* spim/process/cuda/CUDAFourierConvolution.java:31, called from
+ * MVDeconFFTThreads.java:86-89,109-112 and LRFFTThreads.java:70,85.
+ * Convolves the block `im` (imDim = {z,y,x}) in place with `kernel` (kernelDim = {z,y,x},
+ * odd sizes, centre at size/2): true convolution of the block extended mirror-single at its
+ * border, the result the CPU FFTConvolution gives on the same block.  Callers consume the
+ * interior [k/2, dim - k/2).  Synchronous; no pointer is kept.  On failure `im` is left
+ * unmodified and the reason is available from mvd_last_error(). */
+void convolution3DfftCUDAInPlace(float* im, int* imDim, float* kernel, int* kernelDim, int devCUDA);
+
+/* ===================== Part 2: additions (status-returning) ===================== */
+
+enum {
+  MVD_OK = 0,
+  MVD_ERR_ARG = 1,     /* invalid argument */
+  MVD_ERR_CUDA = 2,    /* CUDA runtime error (see mvd_last_error) */
+  MVD_ERR_NOMEM = 3,   /* device allocation failed */
+  MVD_ERR_STATE = 4,   /* call not valid in the handle's state */
+  MVD_ERR_INTERNAL = 5
+};
+
+/* PSFTYPE ordinals of spim/process/fusion/deconvolution/MVDeconFFT.java:49 */
+enum {
+  MVD_OPTIMIZATION_II = 0,
+  MVD_OPTIMIZATION_I = 1,
+  MVD_EFFICIENT_BAYESIAN = 2,
+  MVD_INDEPENDENT = 3
+};
+
+/* handle flags */
+enum {
+  MVD_FLAG_PLAIN = 1,    /* reference structure: one block per launch sequence, separate
+                            quotient / update kernels, no graph (the plain FP32 GPU form) */
+  MVD_FLAG_NO_GRAPH = 2  /* batched, fused passes but launched eagerly (no CUDA graph) */
+};
+
+/* Last error message of the calling thread ("" if none). */
+const char* mvd_last_error(void);
+
+/* Library version string. */
+const char* mvd_version(void);
+
+/* Status-returning convolution3DfftCUDAInPlace (same arguments and semantics). */
+int mvd_convolve3d_inplace(float* im, const int* imDim, const float* kernel, const int* kernelDim,
+                           int devCUDA);
+
+/* Device-pointer convolution on `stream` (a cudaStream_t, NULL = the library's stream of
+ * that device): out = ext(in) (*) kernel over dims_xyz.  ext_mode 0 = mirror-single,
+ * 1 = constant ext_value.  in and out must not overlap.  Returns after enqueueing. */
+int mvd_convolve3d_device(const float* in, float* out, const int* dims_xyz, const float* kernel,
+                          const int* kdims_xyz, int ext_mode, float ext_value, int devCUDA,
+                          void* stream);
+
+/* ----- whole-deconvolution handle: MVDeconvolution / MVDeconInput / MVDeconFFT -----
+ * (spim/process/fusion/deconvolution/MVDeconvolution.java:94-211, MVDeconFFT.java:79-324)
+ * mvd_create uploads the views, weights and PSFs, prepares kernel1/kernel2 per PSFTYPE
+ * (MVDeconFFT.init), their spectra and the tile plans, and initialises psi with the average
+ * of the first iteration (MVDeconvolution.java:133-147).  block_xyz selects the reference's
+ * block size for MVD_FLAG_PLAIN (NULL = one block of image + kernel - 1). */
+typedef struct mvd_decon mvd_decon;
+
+int mvd_create(mvd_decon** out, int devCUDA, const int* dims_xyz, int num_views,
+               const float* const* views, const float* const* weights, const float* const* psfs,
+               const int* psf_dims_xyz /* 3 per view */, int psftype, double lambda, int flags,
+               const int* block_xyz);
+int mvd_destroy(mvd_decon* h);
+
+/* One view stage: conv1 -> quotient -> conv2 -> update (MVDeconvolution.java:374-462). */
+int mvd_run_view(mvd_decon* h, int view);
+/* One iteration = every view in order (MVDeconvolution.runIteration, :349-465). */
+int mvd_run_iteration(mvd_decon* h);
+/* `iterations` iterations back to back. */
+int mvd_run(mvd_decon* h, int iterations);
+/* Wait for queued work. */
+int mvd_synchronize(mvd_decon* h);
+
+/* psi in/out (x fastest, N floats).  mvd_get_psi with masked != 0 applies the reference's
+ * final masking (psi = 0 where no view has data, MVDeconvolution.java:201-208) to the copy. */
+int mvd_get_psi(mvd_decon* h, float* psi, int masked);
+int mvd_set_psi(mvd_decon* h, const float* psi);
+/* psi value set by the first iteration (FP64 average). */
+int mvd_get_initial_average(mvd_decon* h, double* avg);
+/* kernel2 of a view (the compound / mirrored kernel), psf-sized. */
+int mvd_get_kernel(mvd_decon* h, int view, int which /* 1 or 2 */, float* out);
+
+/* Per-view statistics of an iteration ("sum change", "max change per pixel",
+ * MVDeconvolution.java:447-457); `iteration` counts from 0, the last 64 are kept. */
+int mvd_get_stats(mvd_decon* h, int iteration, int view, double* sum_change, double* max_change);
+int mvd_get_iteration(mvd_decon* h, int* iteration);
+
+/* Tile plan of a view: tiles per axis, tile size, effective size, padded voxels. */
+int mvd_get_plan(mvd_decon* h, int view, int* tiles_xyz, int* tile_xyz, int* eff_xyz,
+                 long long* padded_voxels);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MVDECON_H */

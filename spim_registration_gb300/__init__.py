@@ -1,0 +1,16 @@
+"""GB300-native multiview Bayesian deconvolution (fiji/SPIM_Registration hot path).
+
+The compute path is ``lib/libFourierConvolutionCUDA.so`` (sm_103a CUDA, C ABI in
+``include/mvdecon.h``); this package holds its build step, the ctypes binding and the
+Python mirror of the reference's Java classes.
+"""
+from .mvdecon import (  # noqa: F401
+    FLAG_NO_GRAPH,
+    FLAG_PLAIN,
+    PSFTYPE,
+    CUDAFourierConvolution,
+    Deconvolution,
+    MVDeconFFT,
+    MVDeconInput,
+    MVDeconvolution,
+)

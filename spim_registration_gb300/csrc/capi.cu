@@ -1,0 +1,749 @@
+// C ABI of libFourierConvolutionCUDA: the reference's JNA entry points and the
+// whole-deconvolution handle.  Every entry point catches exceptions and turns them into a
+// status code plus a per-thread message; nothing is retained across calls except in handles.
+#include <array>
+#include <cstdio>
+#include <map>
+#include <cstring>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "../../include/mvdecon.h"
+#include "engine.h"
+
+using namespace mvd;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string& msg) {
+  g_last_error = msg;
+  return code;
+}
+
+int from_exception() {
+  try {
+    throw;
+  } catch (const CudaError& e) {
+    return fail(e.code == cudaErrorMemoryAllocation ? MVD_ERR_NOMEM : MVD_ERR_CUDA, e.what());
+  } catch (const std::invalid_argument& e) {
+    return fail(MVD_ERR_ARG, e.what());
+  } catch (const std::bad_alloc&) {
+    return fail(MVD_ERR_NOMEM, "host allocation failed");
+  } catch (const std::exception& e) {
+    return fail(MVD_ERR_INTERNAL, e.what());
+  } catch (...) {
+    return fail(MVD_ERR_INTERNAL, "unknown error");
+  }
+}
+
+#define MVD_API_BEGIN try {
+#define MVD_API_END \
+  }                 \
+  catch (...) { return from_exception(); }
+
+uint64_t fnv1a(const void* data, size_t bytes, uint64_t h = 1469598103934665603ULL) {
+  const unsigned char* p = static_cast<const unsigned char*>(data);
+  for (size_t i = 0; i < bytes; ++i) {
+    h ^= p[i];
+    h *= 1099511628211ULL;
+  }
+  return h;
+}
+
+// Per-device state of the drop-in convolution: stream, plans, cached kernel spectra.
+struct DeviceCtx {
+  std::mutex mu;
+  int dev = -1;
+  cudaStream_t stream = nullptr;
+  PlanTable pt;
+  std::map<std::vector<int>, std::unique_ptr<ConvPlan>> plans;
+  struct Otf {
+    DevBuf buf;
+    uint64_t stamp;
+  };
+  std::map<std::vector<uint64_t>, Otf> otfs;
+  uint64_t clock = 0;
+  DevBuf d_in, d_out, d_spec, d_kernel, scratch;
+
+  ConvPlan& plan_for(int nx, int ny, int nz, int kx, int ky, int kz) {
+    std::vector<int> key{nx, ny, nz, kx, ky, kz};
+    auto it = plans.find(key);
+    if (it != plans.end()) return *it->second;
+    auto p = make_conv_plan(pt, nx, ny, nz, kx, ky, kz);
+    ConvPlan& ref = *p;
+    plans[key] = std::move(p);
+    return ref;
+  }
+
+  // spectrum of a host kernel for a plan, cached by content (the Java side re-sends the same
+  // kernel with every block: MVDeconFFTThreads.java:86-89)
+  const float2* otf_for(const ConvPlan& plan, const float* host_kernel) {
+    const size_t kn = (size_t)plan.kx * plan.ky * plan.kz;
+    std::vector<uint64_t> key{fnv1a(host_kernel, kn * sizeof(float)), (uint64_t)plan.kx, (uint64_t)plan.ky,
+                              (uint64_t)plan.kz, (uint64_t)plan.ax.T, (uint64_t)plan.ay.T, (uint64_t)plan.az.T};
+    auto it = otfs.find(key);
+    if (it != otfs.end()) {
+      it->second.stamp = ++clock;
+      return it->second.buf.as<float2>();
+    }
+    if (otfs.size() >= 16) {  // evict the least recently used spectrum
+      auto victim = otfs.begin();
+      for (auto i = otfs.begin(); i != otfs.end(); ++i)
+        if (i->second.stamp < victim->second.stamp) victim = i;
+      otfs.erase(victim);
+    }
+    d_kernel.ensure(kn * sizeof(float));
+    MVD_CHECK(cudaMemcpyAsync(d_kernel.p, host_kernel, kn * sizeof(float), cudaMemcpyHostToDevice, stream));
+    Otf o;
+    o.buf.alloc(plan.otf_elems * sizeof(float2));
+    build_otf(pt, plan, d_kernel.as<float>(), o.buf.as<float2>(), scratch, stream);
+    o.stamp = ++clock;
+    auto& slot = otfs[key];
+    slot = std::move(o);
+    return slot.buf.as<float2>();
+  }
+};
+
+std::mutex g_ctx_mu;
+std::unordered_map<int, std::unique_ptr<DeviceCtx>> g_ctx;
+
+DeviceCtx& ctx_for(int dev) {
+  int count = 0;
+  MVD_CHECK(cudaGetDeviceCount(&count));
+  if (dev < 0 || dev >= count) throw std::invalid_argument("invalid CUDA device id");
+  std::lock_guard<std::mutex> lk(g_ctx_mu);
+  auto& slot = g_ctx[dev];
+  if (!slot) {
+    auto c = std::make_unique<DeviceCtx>();
+    c->dev = dev;
+    MVD_CHECK(cudaSetDevice(dev));
+    MVD_CHECK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    slot = std::move(c);
+  }
+  return *slot;
+}
+
+void check_dims(const int* d, const char* what) {
+  if (!d) throw std::invalid_argument(std::string(what) + " is NULL");
+  for (int i = 0; i < 3; ++i)
+    if (d[i] < 1) throw std::invalid_argument(std::string(what) + " has a non-positive size");
+}
+
+}  // namespace
+
+// =========================================================================================
+// Part 1: JNA interface
+// =========================================================================================
+extern "C" int getNumDevicesCUDA(void) {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess) {
+    cudaGetLastError();
+    return -1;
+  }
+  return n;
+}
+
+extern "C" int getCUDAcomputeCapabilityMajorVersion(int dev) {
+  int v = -1;
+  if (cudaDeviceGetAttribute(&v, cudaDevAttrComputeCapabilityMajor, dev) != cudaSuccess) return -1;
+  return v;
+}
+
+extern "C" int getCUDAcomputeCapabilityMinorVersion(int dev) {
+  int v = -1;
+  if (cudaDeviceGetAttribute(&v, cudaDevAttrComputeCapabilityMinor, dev) != cudaSuccess) return -1;
+  return v;
+}
+
+extern "C" void getNameDeviceCUDA(int dev, char* name) {
+  if (!name) return;
+  cudaDeviceProp prop;
+  if (cudaGetDeviceProperties(&prop, dev) != cudaSuccess) {
+    std::snprintf(name, 256, "unknown device %d", dev);
+    return;
+  }
+  std::snprintf(name, 256, "%s", prop.name);
+}
+
+extern "C" long long getMemDeviceCUDA(int dev) {
+  cudaDeviceProp prop;
+  if (cudaGetDeviceProperties(&prop, dev) != cudaSuccess) return -1;
+  return (long long)prop.totalGlobalMem;
+}
+
+extern "C" long long getFreeMemDeviceCUDA(int dev) {
+  int prev = 0;
+  cudaGetDevice(&prev);
+  if (cudaSetDevice(dev) != cudaSuccess) return -1;
+  size_t fr = 0, tot = 0;
+  cudaError_t e = cudaMemGetInfo(&fr, &tot);
+  cudaSetDevice(prev);
+  return e == cudaSuccess ? (long long)fr : -1;
+}
+
+extern "C" float* convolution3DfftCUDA(float*, int*, float*, int*, int) {
+  fail(MVD_ERR_STATE, "convolution3DfftCUDA is not provided; use convolution3DfftCUDAInPlace");
+  std::fprintf(stderr, "[FourierConvolutionCUDA] convolution3DfftCUDA is not provided; use convolution3DfftCUDAInPlace\n");
+  return nullptr;
+}
+
+extern "C" const char* mvd_last_error(void) { return g_last_error.c_str(); }
+
+extern "C" const char* mvd_version(void) { return "mvdecon-gb300 0.1 (sm_103a)"; }
+
+extern "C" int mvd_convolve3d_inplace(float* im, const int* imDim, const float* kernel, const int* kernelDim,
+                                      int devCUDA) {
+  MVD_API_BEGIN
+  g_last_error.clear();
+  check_dims(imDim, "imDim");
+  check_dims(kernelDim, "kernelDim");
+  if (!im || !kernel) return fail(MVD_ERR_ARG, "NULL image or kernel");
+  const int nz = imDim[0], ny = imDim[1], nx = imDim[2];     // reversed: {z, y, x}
+  const int kz = kernelDim[0], ky = kernelDim[1], kx = kernelDim[2];
+  if (!(kx & 1) || !(ky & 1) || !(kz & 1)) return fail(MVD_ERR_ARG, "kernel sizes must be odd");
+  DeviceCtx& c = ctx_for(devCUDA);
+  std::lock_guard<std::mutex> lk(c.mu);
+  MVD_CHECK(cudaSetDevice(devCUDA));
+  ConvPlan& plan = c.plan_for(nx, ny, nz, kx, ky, kz);
+  const size_t n = (size_t)nx * ny * nz;
+  c.d_in.ensure(n * sizeof(float));
+  c.d_out.ensure(n * sizeof(float));
+  c.d_spec.ensure(plan.spec_elems * sizeof(float2));
+  MVD_CHECK(cudaMemcpyAsync(c.d_in.p, im, n * sizeof(float), cudaMemcpyHostToDevice, c.stream));
+  const float2* otf = c.otf_for(plan, kernel);
+  convolve(c.pt, plan, c.d_in.as<float>(), Ext::Mirror, 0.f, otf, c.d_spec.as<float2>(), c.d_out.as<float>(),
+           c.stream);
+  // results only reach `im` once everything succeeded
+  std::vector<float> tmp(n);
+  MVD_CHECK(cudaMemcpyAsync(tmp.data(), c.d_out.p, n * sizeof(float), cudaMemcpyDeviceToHost, c.stream));
+  MVD_CHECK(cudaStreamSynchronize(c.stream));
+  std::memcpy(im, tmp.data(), n * sizeof(float));
+  return MVD_OK;
+  MVD_API_END
+}
+
+extern "C" void convolution3DfftCUDAInPlace(float* im, int* imDim, float* kernel, int* kernelDim, int devCUDA) {
+  const int st = mvd_convolve3d_inplace(im, imDim, kernel, kernelDim, devCUDA);
+  if (st != MVD_OK)
+    std::fprintf(stderr, "[FourierConvolutionCUDA] convolution3DfftCUDAInPlace failed (%d): %s\n", st,
+                 g_last_error.c_str());
+}
+
+extern "C" int mvd_convolve3d_device(const float* in, float* out, const int* dims, const float* kernel,
+                                     const int* kdims, int ext_mode, float ext_value, int devCUDA, void* stream) {
+  MVD_API_BEGIN
+  g_last_error.clear();
+  check_dims(dims, "dims_xyz");
+  check_dims(kdims, "kdims_xyz");
+  if (!in || !out || !kernel) return fail(MVD_ERR_ARG, "NULL pointer");
+  if (ext_mode != 0 && ext_mode != 1) return fail(MVD_ERR_ARG, "ext_mode must be 0 or 1");
+  if (!(kdims[0] & 1) || !(kdims[1] & 1) || !(kdims[2] & 1)) return fail(MVD_ERR_ARG, "kernel sizes must be odd");
+  DeviceCtx& c = ctx_for(devCUDA);
+  std::lock_guard<std::mutex> lk(c.mu);
+  MVD_CHECK(cudaSetDevice(devCUDA));
+  cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : c.stream;
+  ConvPlan& plan = c.plan_for(dims[0], dims[1], dims[2], kdims[0], kdims[1], kdims[2]);
+  c.d_spec.ensure(plan.spec_elems * sizeof(float2));
+  DevBuf otf(plan.otf_elems * sizeof(float2));
+  build_otf(c.pt, plan, kernel, otf.as<float2>(), c.scratch, s);
+  convolve(c.pt, plan, in, ext_mode == 0 ? Ext::Mirror : Ext::Value, ext_value, otf.as<float2>(),
+           c.d_spec.as<float2>(), out, s);
+  // the spectrum buffers are reused by the next call: finish before returning
+  MVD_CHECK(cudaStreamSynchronize(s));
+  return MVD_OK;
+  MVD_API_END
+}
+
+// =========================================================================================
+// Part 2: deconvolution handle
+// =========================================================================================
+namespace {
+
+constexpr int kHist = 64;
+
+struct StatSlot {
+  double sum;
+  unsigned max_bits;
+  unsigned pad;
+};
+
+__global__ void archive_stats_kernel(StatSlot* slot, double* hist, const int* iter, int view, int nviews) {
+  const int it = *iter % kHist;
+  hist[(it * nviews + view) * 2 + 0] = slot->sum;
+  hist[(it * nviews + view) * 2 + 1] = (double)__uint_as_float(slot->max_bits);
+}
+
+__global__ void advance_iter_kernel(int* iter) { *iter += 1; }
+
+struct Block {
+  int off[3], eoff[3], esz[3], local[3];
+};
+
+// BlockGeneratorFixedSizePrecise.divideIntoBlocks (BlockGeneratorFixedSizePrecise.java:46-122)
+std::vector<Block> divide_into_blocks(const int img[3], const int k[3], const int b[3]) {
+  int eff[3], nb[3];
+  for (int d = 0; d < 3; ++d) {
+    eff[d] = b[d] - k[d] + 1;
+    if (eff[d] <= 0) throw std::invalid_argument("block size smaller than the kernel");
+    nb[d] = img[d] / eff[d] + (img[d] % eff[d] ? 1 : 0);
+  }
+  std::vector<Block> out;
+  for (int z = 0; z < nb[2]; ++z)
+    for (int y = 0; y < nb[1]; ++y)
+      for (int x = 0; x < nb[0]; ++x) {
+        const int cur[3] = {x, y, z};
+        Block bl;
+        for (int d = 0; d < 3; ++d) {
+          bl.eoff[d] = cur[d] * eff[d];
+          bl.off[d] = bl.eoff[d] - k[d] / 2;
+          bl.esz[d] = std::min(eff[d], img[d] - bl.eoff[d]);
+          bl.local[d] = k[d] / 2;
+        }
+        out.push_back(bl);
+      }
+  return out;
+}
+
+}  // namespace
+
+struct mvd_decon {
+  int dev = 0;
+  cudaStream_t stream = nullptr;
+  PlanTable pt;
+  int dims[3] = {0, 0, 0};
+  long long N = 0;
+  int V = 0;
+  int psftype = 0;
+  float lambda = 0.f;
+  int flags = 0;
+  std::vector<std::array<int, 3>> kd;
+  DevBuf psi, q, tmp2, spec, scratch;
+  std::vector<DevBuf> img, w, k1, k2, otf1, otf2;
+  std::vector<std::unique_ptr<ConvPlan>> plans;
+  // plain form
+  int block[3] = {0, 0, 0};
+  std::vector<std::vector<Block>> blocks;
+  std::vector<std::array<int, 3>> block_size;
+  DevBuf blk_in, blk_out;
+  // statistics
+  DevBuf stats, hist, d_iter, d_sc;
+  int iteration = 0;
+  double avg = 0.0;
+  cudaGraphExec_t graph = nullptr;
+
+  ~mvd_decon() {
+    if (graph) cudaGraphExecDestroy(graph);
+    if (stream) cudaStreamDestroy(stream);
+  }
+
+  StatSlot* slot(int v) { return stats.as<StatSlot>() + v; }
+
+  void enqueue_view(int v) {
+    cudaStream_t s = stream;
+    MVD_CHECK(cudaMemsetAsync(slot(v), 0, sizeof(StatSlot), s));
+    if (flags & MVD_FLAG_PLAIN) {
+      enqueue_view_plain(v);
+    } else {
+      const ConvPlan& p = *plans[v];
+      float2* sp = spec.as<float2>();
+      launch_fwd_mirror(pt, p, psi.as<float>(), sp, s);
+      launch_z(pt, p, sp, otf1[v].as<float2>(), s);
+      launch_inv_quotient(pt, p, sp, img[v].as<float>(), q.as<float>(), s);
+      launch_fwd_value(pt, p, q.as<float>(), 1.f, sp, s);
+      launch_z(pt, p, sp, otf2[v].as<float2>(), s);
+      launch_inv_update(pt, p, sp, psi.as<float>(), w[v].as<float>(), lambda, &slot(v)->sum, &slot(v)->max_bits, s);
+    }
+    archive_stats_kernel<<<1, 1, 0, s>>>(slot(v), hist.as<double>(), d_iter.as<int>(), v, V);
+    MVD_CHECK(cudaGetLastError());
+  }
+
+  // one block per launch sequence: copy block -> 3 FFT passes -> paste (MVDeconFFT.java:438-446,
+  // 528-535, MVDeconFFTThreads.java:73-115), then separate quotient / update kernels
+  void plain_conv(int v, const float* src, Ext ext, float value, const float2* otf, float* dst) {
+    const ConvPlan& p = *plans[v];
+    const auto& bs = block_size[v];
+    for (const Block& b : blocks[v]) {
+      dev_copy_block(src, dims[0], dims[1], dims[2], blk_in.as<float>(), bs[0], bs[1], bs[2], b.off[0], b.off[1],
+                     b.off[2], ext, value, stream);
+      convolve(pt, p, blk_in.as<float>(), Ext::Mirror, 0.f, otf, spec.as<float2>(), blk_out.as<float>(), stream);
+      dev_paste_block(blk_out.as<float>(), bs[0], bs[1], bs[2], b.local[0], b.local[1], b.local[2], dst, dims[0],
+                      dims[1], dims[2], b.eoff[0], b.eoff[1], b.eoff[2], b.esz[0], b.esz[1], b.esz[2], stream);
+    }
+  }
+
+  void enqueue_view_plain(int v) {
+    plain_conv(v, psi.as<float>(), Ext::Mirror, 0.f, otf1[v].as<float2>(), q.as<float>());
+    dev_quotient(q.as<float>(), img[v].as<float>(), N, stream);
+    plain_conv(v, q.as<float>(), Ext::Value, 1.f, otf2[v].as<float2>(), tmp2.as<float>());
+    dev_update(psi.as<float>(), tmp2.as<float>(), w[v].as<float>(), lambda, N, &slot(v)->sum, &slot(v)->max_bits,
+               stream);
+  }
+
+  void enqueue_iteration() {
+    for (int v = 0; v < V; ++v) enqueue_view(v);
+    advance_iter_kernel<<<1, 1, 0, stream>>>(d_iter.as<int>());
+    MVD_CHECK(cudaGetLastError());
+  }
+
+  void run_iteration() {
+    const bool use_graph = !(flags & (MVD_FLAG_PLAIN | MVD_FLAG_NO_GRAPH));
+    if (use_graph) {
+      if (!graph) {
+        pt.device();  // no synchronous uploads may happen during capture
+        cudaGraph_t g = nullptr;
+        MVD_CHECK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+        try {
+          enqueue_iteration();
+        } catch (...) {
+          cudaStreamEndCapture(stream, &g);
+          if (g) cudaGraphDestroy(g);
+          throw;
+        }
+        MVD_CHECK(cudaStreamEndCapture(stream, &g));
+        cudaError_t e = cudaGraphInstantiate(&graph, g, 0);
+        cudaGraphDestroy(g);
+        MVD_CHECK(e);
+      }
+      MVD_CHECK(cudaGraphLaunch(graph, stream));
+    } else {
+      enqueue_iteration();
+    }
+    ++iteration;
+  }
+};
+
+namespace {
+
+// small convolution with zero extension for kernel preparation
+DevBuf conv_zero(mvd_decon* h, const float* in, const std::array<int, 3>& d, const float* kern,
+                 const std::array<int, 3>& kd) {
+  auto plan = make_conv_plan(h->pt, d[0], d[1], d[2], kd[0], kd[1], kd[2]);
+  DevBuf otf(plan->otf_elems * sizeof(float2)), spec(plan->spec_elems * sizeof(float2));
+  DevBuf out((size_t)d[0] * d[1] * d[2] * sizeof(float));
+  build_otf(h->pt, *plan, kern, otf.as<float2>(), h->scratch, h->stream);
+  convolve(h->pt, *plan, in, Ext::Value, 0.f, otf.as<float2>(), spec.as<float2>(), out.as<float>(), h->stream);
+  MVD_CHECK(cudaStreamSynchronize(h->stream));
+  return out;
+}
+
+long long vox(const std::array<int, 3>& d) { return (long long)d[0] * d[1] * d[2]; }
+
+// AdjustInput.normImg with an FP64 unit-sum (AdjustInput.java:50-56)
+void norm_dev(mvd_decon* h, float* k, long long n) {
+  DevBuf sum(sizeof(double));
+  MVD_CHECK(cudaMemsetAsync(sum.p, 0, sizeof(double), h->stream));
+  dev_sum_f64(k, n, sum.as<double>(), h->stream);
+  dev_scale_div(k, n, sum.as<double>(), h->stream);
+  MVD_CHECK(cudaStreamSynchronize(h->stream));
+}
+
+DevBuf mirrored(mvd_decon* h, const float* k, const std::array<int, 3>& d) {
+  DevBuf out(vox(d) * sizeof(float));
+  dev_mirror(k, out.as<float>(), d[0], d[1], d[2], h->stream);
+  return out;
+}
+
+// MVDeconFFT.init (MVDeconFFT.java:183-324) for every view, on the GPU
+void prepare_kernels(mvd_decon* h) {
+  const int V = h->V;
+  for (int v = 0; v < V; ++v) norm_dev(h, h->k1[v].as<float>(), vox(h->kd[v]));
+  for (int v = 0; v < V; ++v) {
+    const auto& dv = h->kd[v];
+    const long long nv = vox(dv);
+    DevBuf k2;
+    if (V == 1 || h->psftype == MVD_INDEPENDENT) {
+      k2 = mirrored(h, h->k1[v].as<float>(), dv);
+    } else if (h->psftype == MVD_EFFICIENT_BAYESIAN) {
+      DevBuf tmp = mirrored(h, h->k1[v].as<float>(), dv);
+      for (int wv = 0; wv < V; ++wv) {
+        if (wv == v) continue;
+        DevBuf in = mirrored(h, h->k1[v].as<float>(), dv);
+        DevBuf a = conv_zero(h, in.as<float>(), dv, h->k1[wv].as<float>(), h->kd[wv]);
+        DevBuf mw = mirrored(h, h->k1[wv].as<float>(), h->kd[wv]);
+        DevBuf b = conv_zero(h, a.as<float>(), dv, mw.as<float>(), h->kd[wv]);
+        dev_mul(tmp.as<float>(), b.as<float>(), nv, h->stream);
+      }
+      norm_dev(h, tmp.as<float>(), nv);
+      k2 = std::move(tmp);
+    } else if (h->psftype == MVD_OPTIMIZATION_I) {
+      DevBuf tmp(nv * sizeof(float));
+      MVD_CHECK(cudaMemcpyAsync(tmp.p, h->k1[v].p, nv * sizeof(float), cudaMemcpyDeviceToDevice, h->stream));
+      for (int wv = 0; wv < V; ++wv) {
+        if (wv == v) continue;
+        DevBuf mw = mirrored(h, h->k1[wv].as<float>(), h->kd[wv]);
+        DevBuf a = conv_zero(h, h->k1[v].as<float>(), dv, mw.as<float>(), h->kd[wv]);
+        dev_mul(tmp.as<float>(), a.as<float>(), nv, h->stream);
+      }
+      norm_dev(h, tmp.as<float>(), nv);
+      k2 = mirrored(h, tmp.as<float>(), dv);
+    } else {
+      DevBuf e(nv * sizeof(float));
+      MVD_CHECK(cudaMemcpyAsync(e.p, h->k1[v].p, nv * sizeof(float), cudaMemcpyDeviceToDevice, h->stream));
+      dev_pow(e.as<float>(), V, nv, h->stream);
+      norm_dev(h, e.as<float>(), nv);
+      k2 = mirrored(h, e.as<float>(), dv);
+    }
+    MVD_CHECK(cudaStreamSynchronize(h->stream));
+    h->k2[v] = std::move(k2);
+  }
+}
+
+std::unique_ptr<ConvPlan> block_plan(PlanTable& pt, const std::array<int, 3>& b, const std::array<int, 3>& k) {
+  // the block convolved as a volume (mirror-single at its own border); its interior is what
+  // the paste consumes
+  return make_conv_plan(pt, b[0], b[1], b[2], k[0], k[1], k[2]);
+}
+
+}  // namespace
+
+extern "C" int mvd_create(mvd_decon** out, int devCUDA, const int* dims, int num_views, const float* const* views,
+                          const float* const* weights, const float* const* psfs, const int* psf_dims, int psftype,
+                          double lambda, int flags, const int* block_xyz) {
+  MVD_API_BEGIN
+  g_last_error.clear();
+  if (!out) return fail(MVD_ERR_ARG, "out is NULL");
+  *out = nullptr;
+  check_dims(dims, "dims_xyz");
+  if (num_views < 1 || num_views > 16) return fail(MVD_ERR_ARG, "num_views must be in [1, 16]");
+  if (!views || !weights || !psfs || !psf_dims) return fail(MVD_ERR_ARG, "NULL input array");
+  if (psftype < 0 || psftype > 3) return fail(MVD_ERR_ARG, "unknown psftype");
+  for (int v = 0; v < num_views; ++v) {
+    if (!views[v] || !weights[v] || !psfs[v]) return fail(MVD_ERR_ARG, "NULL view, weight or psf");
+    check_dims(psf_dims + 3 * v, "psf_dims");
+    for (int d = 0; d < 3; ++d)
+      if (!(psf_dims[3 * v + d] & 1)) return fail(MVD_ERR_ARG, "psf sizes must be odd");
+  }
+  if (block_xyz) check_dims(block_xyz, "block_xyz");
+  int count = 0;
+  MVD_CHECK(cudaGetDeviceCount(&count));
+  if (devCUDA < 0 || devCUDA >= count) return fail(MVD_ERR_ARG, "invalid CUDA device id");
+  MVD_CHECK(cudaSetDevice(devCUDA));
+  auto h = std::make_unique<mvd_decon>();
+  h->dev = devCUDA;
+  MVD_CHECK(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+  for (int d = 0; d < 3; ++d) h->dims[d] = dims[d];
+  h->N = (long long)dims[0] * dims[1] * dims[2];
+  h->V = num_views;
+  h->psftype = psftype;
+  h->lambda = (float)lambda;
+  h->flags = flags;
+  const size_t nb = h->N * sizeof(float);
+  h->img.resize(num_views);
+  h->w.resize(num_views);
+  h->k1.resize(num_views);
+  h->k2.resize(num_views);
+  h->otf1.resize(num_views);
+  h->otf2.resize(num_views);
+  for (int v = 0; v < num_views; ++v) {
+    h->kd.push_back({psf_dims[3 * v], psf_dims[3 * v + 1], psf_dims[3 * v + 2]});
+    h->img[v].alloc(nb);
+    h->w[v].alloc(nb);
+    MVD_CHECK(cudaMemcpyAsync(h->img[v].p, views[v], nb, cudaMemcpyHostToDevice, h->stream));
+    MVD_CHECK(cudaMemcpyAsync(h->w[v].p, weights[v], nb, cudaMemcpyHostToDevice, h->stream));
+    const size_t kb = vox(h->kd[v]) * sizeof(float);
+    h->k1[v].alloc(kb);
+    MVD_CHECK(cudaMemcpyAsync(h->k1[v].p, psfs[v], kb, cudaMemcpyHostToDevice, h->stream));
+  }
+  MVD_CHECK(cudaStreamSynchronize(h->stream));
+  prepare_kernels(h.get());
+  h->psi.alloc(nb);
+  h->q.alloc(nb);
+  long long spec_max = 0;
+  if (flags & MVD_FLAG_PLAIN) {
+    h->tmp2.alloc(nb);
+    size_t blk_max = 0;
+    for (int v = 0; v < num_views; ++v) {
+      std::array<int, 3> bs;
+      for (int d = 0; d < 3; ++d) bs[d] = block_xyz ? block_xyz[d] : dims[d] + h->kd[v][d] - 1;
+      h->block_size.push_back(bs);
+      h->blocks.push_back(divide_into_blocks(h->dims, h->kd[v].data(), bs.data()));
+      h->plans.push_back(block_plan(h->pt, bs, h->kd[v]));
+      blk_max = std::max<size_t>(blk_max, (size_t)vox(bs));
+    }
+    h->blk_in.alloc(blk_max * sizeof(float));
+    h->blk_out.alloc(blk_max * sizeof(float));
+  } else {
+    for (int v = 0; v < num_views; ++v)
+      h->plans.push_back(make_conv_plan(h->pt, dims[0], dims[1], dims[2], h->kd[v][0], h->kd[v][1], h->kd[v][2]));
+  }
+  for (int v = 0; v < num_views; ++v) {
+    const ConvPlan& p = *h->plans[v];
+    spec_max = std::max(spec_max, p.spec_elems);
+    h->otf1[v].alloc(p.otf_elems * sizeof(float2));
+    h->otf2[v].alloc(p.otf_elems * sizeof(float2));
+    build_otf(h->pt, p, h->k1[v].as<float>(), h->otf1[v].as<float2>(), h->scratch, h->stream);
+    build_otf(h->pt, p, h->k2[v].as<float>(), h->otf2[v].as<float2>(), h->scratch, h->stream);
+  }
+  h->spec.alloc(spec_max * sizeof(float2));
+  h->scratch.alloc(0);
+  // first iteration: psi := average intensity of the overlapping area
+  h->d_sc.alloc(2 * sizeof(double));
+  MVD_CHECK(cudaMemsetAsync(h->d_sc.p, 0, 2 * sizeof(double), h->stream));
+  std::vector<const float*> vp;
+  for (int v = 0; v < num_views; ++v) vp.push_back(h->img[v].as<float>());
+  dev_first_iteration(vp.data(), num_views, h->N, h->d_sc.as<double>(), h->stream);
+  dev_fill_from_avg(h->psi.as<float>(), h->d_sc.as<double>(), h->N, h->stream);
+  double sc[2];
+  MVD_CHECK(cudaMemcpyAsync(sc, h->d_sc.p, sizeof(sc), cudaMemcpyDeviceToHost, h->stream));
+  h->stats.alloc(num_views * sizeof(StatSlot));
+  h->hist.alloc((size_t)kHist * num_views * 2 * sizeof(double));
+  h->d_iter.alloc(sizeof(int));
+  MVD_CHECK(cudaMemsetAsync(h->stats.p, 0, num_views * sizeof(StatSlot), h->stream));
+  MVD_CHECK(cudaMemsetAsync(h->hist.p, 0, (size_t)kHist * num_views * 2 * sizeof(double), h->stream));
+  MVD_CHECK(cudaMemsetAsync(h->d_iter.p, 0, sizeof(int), h->stream));
+  MVD_CHECK(cudaStreamSynchronize(h->stream));
+  h->avg = sc[0] / sc[1];
+  if (h->avg != h->avg) h->avg = 0.5;
+  *out = h.release();
+  return MVD_OK;
+  MVD_API_END
+}
+
+extern "C" int mvd_destroy(mvd_decon* h) {
+  MVD_API_BEGIN
+  if (!h) return MVD_OK;
+  cudaSetDevice(h->dev);
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  delete h;
+  return MVD_OK;
+  MVD_API_END
+}
+
+extern "C" int mvd_run_view(mvd_decon* h, int view) {
+  MVD_API_BEGIN
+  if (!h) return fail(MVD_ERR_ARG, "NULL handle");
+  if (view < 0 || view >= h->V) return fail(MVD_ERR_ARG, "view out of range");
+  MVD_CHECK(cudaSetDevice(h->dev));
+  h->enqueue_view(view);
+  if (view == h->V - 1) {
+    advance_iter_kernel<<<1, 1, 0, h->stream>>>(h->d_iter.as<int>());
+    MVD_CHECK(cudaGetLastError());
+    ++h->iteration;
+  }
+  return MVD_OK;
+  MVD_API_END
+}
+
+extern "C" int mvd_run_iteration(mvd_decon* h) {
+  MVD_API_BEGIN
+  if (!h) return fail(MVD_ERR_ARG, "NULL handle");
+  MVD_CHECK(cudaSetDevice(h->dev));
+  h->run_iteration();
+  return MVD_OK;
+  MVD_API_END
+}
+
+extern "C" int mvd_run(mvd_decon* h, int iterations) {
+  MVD_API_BEGIN
+  if (!h) return fail(MVD_ERR_ARG, "NULL handle");
+  if (iterations < 0) return fail(MVD_ERR_ARG, "negative iteration count");
+  MVD_CHECK(cudaSetDevice(h->dev));
+  for (int i = 0; i < iterations; ++i) h->run_iteration();
+  return MVD_OK;
+  MVD_API_END
+}
+
+extern "C" int mvd_synchronize(mvd_decon* h) {
+  MVD_API_BEGIN
+  if (!h) return fail(MVD_ERR_ARG, "NULL handle");
+  MVD_CHECK(cudaSetDevice(h->dev));
+  MVD_CHECK(cudaStreamSynchronize(h->stream));
+  return MVD_OK;
+  MVD_API_END
+}
+
+extern "C" int mvd_get_psi(mvd_decon* h, float* psi, int masked) {
+  MVD_API_BEGIN
+  if (!h || !psi) return fail(MVD_ERR_ARG, "NULL argument");
+  MVD_CHECK(cudaSetDevice(h->dev));
+  const size_t nb = h->N * sizeof(float);
+  if (masked) {
+    DevBuf m(nb);
+    MVD_CHECK(cudaMemcpyAsync(m.p, h->psi.p, nb, cudaMemcpyDeviceToDevice, h->stream));
+    std::vector<const float*> vp;
+    for (int v = 0; v < h->V; ++v) vp.push_back(h->img[v].as<float>());
+    dev_mask(m.as<float>(), vp.data(), h->V, h->N, h->stream);
+    MVD_CHECK(cudaMemcpyAsync(psi, m.p, nb, cudaMemcpyDeviceToHost, h->stream));
+    MVD_CHECK(cudaStreamSynchronize(h->stream));
+  } else {
+    MVD_CHECK(cudaMemcpyAsync(psi, h->psi.p, nb, cudaMemcpyDeviceToHost, h->stream));
+    MVD_CHECK(cudaStreamSynchronize(h->stream));
+  }
+  return MVD_OK;
+  MVD_API_END
+}
+
+extern "C" int mvd_set_psi(mvd_decon* h, const float* psi) {
+  MVD_API_BEGIN
+  if (!h || !psi) return fail(MVD_ERR_ARG, "NULL argument");
+  MVD_CHECK(cudaSetDevice(h->dev));
+  MVD_CHECK(cudaMemcpyAsync(h->psi.p, psi, h->N * sizeof(float), cudaMemcpyHostToDevice, h->stream));
+  MVD_CHECK(cudaStreamSynchronize(h->stream));
+  return MVD_OK;
+  MVD_API_END
+}
+
+extern "C" int mvd_get_initial_average(mvd_decon* h, double* avg) {
+  if (!h || !avg) return fail(MVD_ERR_ARG, "NULL argument");
+  *avg = h->avg;
+  return MVD_OK;
+}
+
+extern "C" int mvd_get_kernel(mvd_decon* h, int view, int which, float* out) {
+  MVD_API_BEGIN
+  if (!h || !out) return fail(MVD_ERR_ARG, "NULL argument");
+  if (view < 0 || view >= h->V || (which != 1 && which != 2)) return fail(MVD_ERR_ARG, "bad view or kernel");
+  MVD_CHECK(cudaSetDevice(h->dev));
+  const DevBuf& k = which == 1 ? h->k1[view] : h->k2[view];
+  MVD_CHECK(cudaMemcpyAsync(out, k.p, vox(h->kd[view]) * sizeof(float), cudaMemcpyDeviceToHost, h->stream));
+  MVD_CHECK(cudaStreamSynchronize(h->stream));
+  return MVD_OK;
+  MVD_API_END
+}
+
+extern "C" int mvd_get_stats(mvd_decon* h, int iteration, int view, double* sum_change, double* max_change) {
+  MVD_API_BEGIN
+  if (!h || !sum_change || !max_change) return fail(MVD_ERR_ARG, "NULL argument");
+  if (view < 0 || view >= h->V) return fail(MVD_ERR_ARG, "view out of range");
+  if (iteration < 0 || iteration >= h->iteration + 1 || iteration < h->iteration + 1 - kHist)
+    return fail(MVD_ERR_ARG, "iteration not in the kept history");
+  MVD_CHECK(cudaSetDevice(h->dev));
+  double v2[2];
+  const int it = iteration % kHist;
+  MVD_CHECK(cudaMemcpyAsync(v2, h->hist.as<double>() + (it * h->V + view) * 2, sizeof(v2), cudaMemcpyDeviceToHost,
+                            h->stream));
+  MVD_CHECK(cudaStreamSynchronize(h->stream));
+  *sum_change = v2[0];
+  *max_change = v2[1];
+  return MVD_OK;
+  MVD_API_END
+}
+
+extern "C" int mvd_get_iteration(mvd_decon* h, int* iteration) {
+  if (!h || !iteration) return fail(MVD_ERR_ARG, "NULL argument");
+  *iteration = h->iteration;
+  return MVD_OK;
+}
+
+extern "C" int mvd_get_plan(mvd_decon* h, int view, int* tiles, int* tile, int* eff, long long* padded) {
+  if (!h) return fail(MVD_ERR_ARG, "NULL handle");
+  if (view < 0 || view >= h->V) return fail(MVD_ERR_ARG, "view out of range");
+  const ConvPlan& p = *h->plans[view];
+  const AxisTiles* a[3] = {&p.ax, &p.ay, &p.az};
+  for (int d = 0; d < 3; ++d) {
+    if (tiles) tiles[d] = a[d]->n;
+    if (tile) tile[d] = a[d]->T;
+    if (eff) eff[d] = a[d]->E;
+  }
+  if (padded) {
+    long long pv = p.padded_voxels();
+    if (h->flags & MVD_FLAG_PLAIN) pv *= (long long)h->blocks[view].size();
+    *padded = pv;
+  }
+  return MVD_OK;
+}

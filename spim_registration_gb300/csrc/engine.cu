@@ -1,0 +1,649 @@
+// Host engine of the tiled FFT convolution: plans, tile planner, OTF preparation, launches,
+// and the small elementwise / reduction kernels of the deconvolution path.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <sstream>
+
+#include "engine.h"
+
+namespace mvd {
+
+void check_cuda(cudaError_t e, const char* what) {
+  if (e != cudaSuccess) {
+    std::string msg = std::string(what) + ": " + cudaGetErrorString(e);
+    throw CudaError(e, msg);
+  }
+}
+
+DevBuf::~DevBuf() {
+  if (p) cudaFree(p);
+}
+DevBuf& DevBuf::operator=(DevBuf&& o) noexcept {
+  if (this != &o) {
+    if (p) cudaFree(p);
+    p = o.p;
+    bytes = o.bytes;
+    o.p = nullptr;
+    o.bytes = 0;
+  }
+  return *this;
+}
+void DevBuf::alloc(size_t b) {
+  if (p) cudaFree(p);
+  p = nullptr;
+  bytes = 0;
+  if (b == 0) return;
+  MVD_CHECK(cudaMalloc(&p, b));
+  bytes = b;
+}
+void DevBuf::ensure(size_t b) {
+  if (b > bytes) alloc(b);
+}
+
+bool is_smooth(int n) {
+  if (n <= 0) return false;
+  for (int f : {2, 3, 5, 7})
+    while (n % f == 0) n /= f;
+  return n == 1;
+}
+
+int next_smooth(int n, bool even) {
+  if (n < 2) n = 2;
+  for (int m = n;; ++m) {
+    if (even && (m & 1)) continue;
+    if (is_smooth(m)) return m;
+  }
+}
+
+std::vector<int> factorize(int n) {
+  std::vector<int> r;
+  while (n % 8 == 0) { r.push_back(8); n /= 8; }
+  if (n % 4 == 0) { r.push_back(4); n /= 4; }
+  if (n % 2 == 0) { r.push_back(2); n /= 2; }
+  for (int f : {7, 5, 3})
+    while (n % f == 0) { r.push_back(f); n /= f; }
+  if (n != 1) throw std::invalid_argument("FFT length is not 2,3,5,7-smooth");
+  if (r.empty()) r.push_back(1);
+  return r;
+}
+
+// ------------------------------------------------------------------------------------------
+// plan table
+// ------------------------------------------------------------------------------------------
+int PlanTable::index_of(int n) {
+  auto it = by_len_.find(n);
+  if (it != by_len_.end()) return it->second;
+  if (n < 1) throw std::invalid_argument("bad FFT length");
+  if ((int)host_.size() >= kCapacity) throw std::runtime_error("FFT plan table full");
+  FftPlan p{};
+  p.n = n;
+  std::vector<int> rad = (n == 1) ? std::vector<int>{} : factorize(n);
+  if ((int)rad.size() > kMaxStages) throw std::invalid_argument("too many FFT stages");
+  p.nstages = (int)rad.size();
+  for (size_t i = 0; i < rad.size(); ++i) p.radix[i] = rad[i];
+  // twiddles: [0, n) for the complex length n, then [0, n] for the real length 2n
+  std::vector<float2> tw(2 * n + 1);
+  for (int k = 0; k < n; ++k) {
+    const double a = -2.0 * M_PI * (double)k / (double)n;
+    tw[k] = make_float2((float)std::cos(a), (float)std::sin(a));
+  }
+  for (int k = 0; k <= n; ++k) {
+    const double a = -M_PI * (double)k / (double)n;
+    tw[n + k] = make_float2((float)std::cos(a), (float)std::sin(a));
+  }
+  auto buf = std::make_unique<DevBuf>(tw.size() * sizeof(float2));
+  MVD_CHECK(cudaMemcpy(buf->p, tw.data(), tw.size() * sizeof(float2), cudaMemcpyHostToDevice));
+  p.tw = buf->as<float2>();
+  p.tw_r2c = buf->as<float2>() + n;
+  tw_bufs_.push_back(std::move(buf));
+  const int idx = (int)host_.size();
+  host_.push_back(p);
+  by_len_[n] = idx;
+  dirty_ = true;
+  return idx;
+}
+
+const FftPlan* PlanTable::device() {
+  if (!dev_.p) dev_.alloc(kCapacity * sizeof(FftPlan));
+  if (dirty_) {
+    // append-only table at a fixed address: entries already in use never change, so kernels
+    // (and captured graphs) holding this pointer stay valid while new lengths are added
+    MVD_CHECK(cudaMemcpy(dev_.p, host_.data(), host_.size() * sizeof(FftPlan), cudaMemcpyHostToDevice));
+    dirty_ = false;
+  }
+  return dev_.as<FftPlan>();
+}
+
+// ------------------------------------------------------------------------------------------
+// tile planner
+// ------------------------------------------------------------------------------------------
+static std::vector<AxisTiles> axis_options(int size, int k, bool even, int tmax) {
+  std::vector<AxisTiles> out;
+  int last_T = -1;
+  const int nmax = std::max(1, size);
+  for (int n = 1; n <= nmax && n <= 64; ++n) {
+    const int need = (size + n - 1) / n + k - 1;
+    int T = next_smooth(std::max(need, k), even);
+    if (T > tmax) continue;
+    if (T == last_T) continue;
+    last_T = T;
+    AxisTiles a;
+    a.size = size;
+    a.k = k;
+    a.T = T;
+    a.E = T - k + 1;
+    a.n = (size + a.E - 1) / a.E;
+    out.push_back(a);
+    if (a.E < 8 && a.E < size) break;  // smaller tiles would be nearly all halo
+  }
+  return out;
+}
+
+static void fill_items(ConvPlan& p) {
+  p.items_fwd.clear();
+  p.items_inv.clear();
+  p.items_z.clear();
+  for (int i = 0; i < (int)p.tiles.size(); ++i) {
+    const TileDesc& t = p.tiles[i];
+    for (int z = 0; z < t.tz; ++z) p.items_fwd.push_back(make_int2(i, z));
+    for (int z = t.hz; z < t.hz + t.ez; ++z) p.items_inv.push_back(make_int2(i, z));
+    const int plane = t.ty * t.px;
+    for (int p0 = 0; p0 < plane; p0 += kZChunk) p.items_z.push_back(make_int2(i, p0));
+  }
+}
+
+void ConvPlan::upload() {
+  d_tiles.alloc(tiles.size() * sizeof(TileDesc));
+  MVD_CHECK(cudaMemcpy(d_tiles.p, tiles.data(), tiles.size() * sizeof(TileDesc), cudaMemcpyHostToDevice));
+  auto up = [](DevBuf& b, const std::vector<int2>& v) {
+    b.alloc(std::max<size_t>(1, v.size()) * sizeof(int2));
+    if (!v.empty()) MVD_CHECK(cudaMemcpy(b.p, v.data(), v.size() * sizeof(int2), cudaMemcpyHostToDevice));
+  };
+  up(d_items_fwd, items_fwd);
+  up(d_items_inv, items_inv);
+  up(d_items_z, items_z);
+}
+
+std::unique_ptr<ConvPlan> make_conv_plan(PlanTable& pt, int nx, int ny, int nz, int kx, int ky,
+                                         int kz, const PlanOptions& opt) {
+  if (nx < 1 || ny < 1 || nz < 1) throw std::invalid_argument("empty volume");
+  if (kx < 1 || ky < 1 || kz < 1 || !(kx & 1) || !(ky & 1) || !(kz & 1))
+    throw std::invalid_argument("kernel sizes must be odd and positive");
+  auto opts = [&](int size, int k, bool even, int tmax, int force) {
+    if (force > 0) {
+      AxisTiles a;
+      a.size = size;
+      a.k = k;
+      a.T = force;
+      a.E = force - k + 1;
+      if (a.E <= 0 || (even && (force & 1)) || !is_smooth(even ? force / 2 : force))
+        throw std::invalid_argument("forced tile size is too small or not smooth");
+      a.n = (size + a.E - 1) / a.E;
+      return std::vector<AxisTiles>{a};
+    }
+    return axis_options(size, k, even, tmax);
+  };
+  auto ox = opts(nx, kx, true, 2 * (kPlaneCap / 8), opt.force_tx);
+  auto oy = opts(ny, ky, false, kPlaneCap / 2, opt.force_ty);
+  auto oz = opts(nz, kz, false, kPlaneCap / kZPitch, opt.force_tz);
+  double best = 1e300;
+  AxisTiles bx, by, bz;
+  for (auto& a : ox)
+    for (auto& b : oy) {
+      const int pxa = a.T / 2 + 1;
+      if ((long long)((pxa & 1) ? pxa : pxa + 1) * b.T > kPlaneCap) continue;
+      for (auto& c : oz) {
+        const double ntiles = (double)a.n * b.n * c.n;
+        const double cost = ntiles * a.T * b.T * c.T * (1.0 + 1e-3 * ntiles);
+        if (cost < best) {
+          best = cost;
+          bx = a;
+          by = b;
+          bz = c;
+        }
+      }
+    }
+  if (best >= 1e300) throw std::invalid_argument("no tile shape fits this kernel (kernel too large)");
+  auto plan = std::make_unique<ConvPlan>();
+  ConvPlan& p = *plan;
+  p.nx = nx; p.ny = ny; p.nz = nz;
+  p.kx = kx; p.ky = ky; p.kz = kz;
+  p.ax = bx; p.ay = by; p.az = bz;
+  const int px = bx.T / 2 + 1;
+  const int pitch = (px & 1) ? px : px + 1;
+  const int plx = pt.index_of(bx.T / 2), ply = pt.index_of(by.T), plz = pt.index_of(bz.T);
+  const long long tile_spec = (long long)px * by.T * bz.T;
+  long long off = 0;
+  for (int iz = 0; iz < bz.n; ++iz)
+    for (int iy = 0; iy < by.n; ++iy)
+      for (int ix = 0; ix < bx.n; ++ix) {
+        TileDesc t{};
+        t.tx = bx.T; t.ty = by.T; t.tz = bz.T;
+        t.px = px;
+        t.pitch = pitch;
+        t.hx = kx / 2; t.hy = ky / 2; t.hz = kz / 2;
+        const int ex0 = ix * bx.E, ey0 = iy * by.E, ez0 = iz * bz.E;
+        t.ox = ex0 - kx / 2; t.oy = ey0 - ky / 2; t.oz = ez0 - kz / 2;
+        t.ex = std::min(bx.E, nx - ex0);
+        t.ey = std::min(by.E, ny - ey0);
+        t.ez = std::min(bz.E, nz - ez0);
+        t.plan_x = plx; t.plan_y = ply; t.plan_z = plz;
+        t.spec_off = off;
+        t.otf_off = 0;
+        off += tile_spec;
+        p.tiles.push_back(t);
+      }
+  p.spec_elems = off;
+  p.otf_elems = tile_spec;
+  p.smem_plane = 2 * (size_t)by.T * pitch * sizeof(float2);
+  p.smem_z = 2 * (size_t)bz.T * kZPitch * sizeof(float2);
+  fill_items(p);
+  p.upload();
+  return plan;
+}
+
+std::string describe(const ConvPlan& p) {
+  std::ostringstream os;
+  os << "volume " << p.nx << "x" << p.ny << "x" << p.nz << " kernel " << p.kx << "x" << p.ky << "x"
+     << p.kz << " tiles " << p.ax.n << "x" << p.ay.n << "x" << p.az.n << " of " << p.ax.T << "x"
+     << p.ay.T << "x" << p.az.T << " (effective " << p.ax.E << "x" << p.ay.E << "x" << p.az.E
+     << "), padded/volume " << (double)p.padded_voxels() / ((double)p.nx * p.ny * p.nz);
+  return os.str();
+}
+
+// ------------------------------------------------------------------------------------------
+// launches
+// ------------------------------------------------------------------------------------------
+// raise a kernel's dynamic shared-memory limit once per (device, kernel, size)
+static void set_smem_raw(const void* kernel, size_t bytes) {
+  static std::mutex mu;
+  static std::map<std::pair<int, const void*>, size_t> done;
+  int dev = 0;
+  MVD_CHECK(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lk(mu);
+  auto key = std::make_pair(dev, kernel);
+  auto it = done.find(key);
+  if (it != done.end() && it->second >= bytes) return;
+  MVD_CHECK(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+  done[key] = bytes;
+}
+template <class K>
+static void set_smem(K kernel, size_t bytes) {
+  set_smem_raw(reinterpret_cast<const void*>(kernel), bytes);
+}
+
+template <class Gather>
+static void launch_fwd_impl(PlanTable& pt, const ConvPlan& p, const TileDesc* tiles, const int2* items,
+                            int nitems, size_t smem, float2* spec, Gather g, cudaStream_t s) {
+  if (nitems == 0) return;
+  auto k = plane_fwd_kernel<Gather>;
+  set_smem(k, smem);
+  k<<<nitems, kThreads, smem, s>>>(tiles, items, pt.device(), spec, g);
+  MVD_CHECK(cudaGetLastError());
+}
+
+template <class Epi>
+static void launch_inv_impl(PlanTable& pt, const ConvPlan& p, const float2* spec, Epi e, cudaStream_t s) {
+  if (p.items_inv.empty()) return;
+  auto k = plane_inv_kernel<Epi>;
+  set_smem(k, p.smem_plane);
+  k<<<(int)p.items_inv.size(), kThreads, p.smem_plane, s>>>(p.d_tiles.as<TileDesc>(),
+                                                             p.d_items_inv.as<int2>(), pt.device(), spec, e);
+  MVD_CHECK(cudaGetLastError());
+}
+
+void launch_fwd_mirror(PlanTable& pt, const ConvPlan& p, const float* vol, float2* spec, cudaStream_t s) {
+  GatherMirror g{{vol, p.nx, p.ny, p.nz}};
+  launch_fwd_impl(pt, p, p.d_tiles.as<TileDesc>(), p.d_items_fwd.as<int2>(), (int)p.items_fwd.size(),
+                  p.smem_plane, spec, g, s);
+}
+
+void launch_fwd_value(PlanTable& pt, const ConvPlan& p, const float* vol, float value, float2* spec,
+                      cudaStream_t s) {
+  GatherValue g{{vol, p.nx, p.ny, p.nz}, value};
+  launch_fwd_impl(pt, p, p.d_tiles.as<TileDesc>(), p.d_items_fwd.as<int2>(), (int)p.items_fwd.size(),
+                  p.smem_plane, spec, g, s);
+}
+
+void launch_z(PlanTable& pt, const ConvPlan& p, float2* spec, const float2* otf, cudaStream_t s) {
+  if (p.items_z.empty()) return;
+  auto k = zpass_kernel<0>;
+  set_smem(k, p.smem_z);
+  k<<<(int)p.items_z.size(), kThreads, p.smem_z, s>>>(p.d_tiles.as<TileDesc>(), p.d_items_z.as<int2>(),
+                                                       pt.device(), spec, otf, 1.f);
+  MVD_CHECK(cudaGetLastError());
+}
+
+void launch_inv_store(PlanTable& pt, const ConvPlan& p, const float2* spec, float* out, cudaStream_t s) {
+  EpiStore e{out, p.nx, p.ny};
+  launch_inv_impl(pt, p, spec, e, s);
+}
+
+void launch_inv_quotient(PlanTable& pt, const ConvPlan& p, const float2* spec, const float* img,
+                         float* q, cudaStream_t s) {
+  EpiQuotient e{img, q, p.nx, p.ny};
+  launch_inv_impl(pt, p, spec, e, s);
+}
+
+void launch_inv_update(PlanTable& pt, const ConvPlan& p, const float2* spec, float* psi,
+                       const float* weight, float lambda, double* stat_sum, unsigned* stat_max,
+                       cudaStream_t s) {
+  EpiUpdate e{psi, weight, lambda, stat_sum, stat_max, p.nx, p.ny, 0.f, 0.f};
+  launch_inv_impl(pt, p, spec, e, s);
+}
+
+void convolve(PlanTable& pt, const ConvPlan& plan, const float* in, Ext ext, float value,
+              const float2* otf, float2* spec, float* out, cudaStream_t s) {
+  if (ext == Ext::Mirror)
+    launch_fwd_mirror(pt, plan, in, spec, s);
+  else
+    launch_fwd_value(pt, plan, in, value, spec, s);
+  launch_z(pt, plan, spec, otf, s);
+  launch_inv_store(pt, plan, spec, out, s);
+}
+
+// ------------------------------------------------------------------------------------------
+// OTF: kernel placed with its centre at the tile origin (wrap-around), forward 3D FFT,
+// scaled by 1 / (tx ty tz) so that the unnormalised inverse transforms give the convolution.
+// ------------------------------------------------------------------------------------------
+__global__ void place_kernel_kernel(const float* __restrict__ k, int kx, int ky, int kz, float* __restrict__ vol,
+                                    int tx, int ty, int tz) {
+  const long long n = (long long)kx * ky * kz;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const int x = (int)(i % kx);
+    const int y = (int)((i / kx) % ky);
+    const int z = (int)(i / ((long long)kx * ky));
+    const int wx = ((x - kx / 2) % tx + tx) % tx;
+    const int wy = ((y - ky / 2) % ty + ty) % ty;
+    const int wz = ((z - kz / 2) % tz + tz) % tz;
+    vol[((long long)wz * ty + wy) * tx + wx] = k[i];
+  }
+}
+
+void build_otf(PlanTable& pt, const ConvPlan& plan, const float* kernel, float2* otf, DevBuf& scratch,
+               cudaStream_t s) {
+  const int tx = plan.ax.T, ty = plan.ay.T, tz = plan.az.T;
+  if (plan.kx > tx || plan.ky > ty || plan.kz > tz) throw std::invalid_argument("kernel larger than tile");
+  const size_t vox = (size_t)tx * ty * tz;
+  scratch.ensure(vox * sizeof(float));
+  MVD_CHECK(cudaMemsetAsync(scratch.p, 0, vox * sizeof(float), s));
+  const long long kn = (long long)plan.kx * plan.ky * plan.kz;
+  place_kernel_kernel<<<(int)std::min<long long>((kn + 255) / 256, 4096), 256, 0, s>>>(
+      kernel, plan.kx, plan.ky, plan.kz, scratch.as<float>(), tx, ty, tz);
+  MVD_CHECK(cudaGetLastError());
+  // one tile covering the placed kernel volume exactly; its spectrum goes to `otf`
+  TileDesc t = plan.tiles[0];
+  t.ox = t.oy = t.oz = 0;
+  t.hx = t.hy = t.hz = 0;
+  t.ex = tx; t.ey = ty; t.ez = tz;
+  t.spec_off = 0;
+  t.otf_off = 0;
+  std::vector<int2> fwd, zz;
+  for (int z = 0; z < tz; ++z) fwd.push_back(make_int2(0, z));
+  for (int p0 = 0; p0 < ty * t.px; p0 += kZChunk) zz.push_back(make_int2(0, p0));
+  DevBuf dt(sizeof(TileDesc)), df(fwd.size() * sizeof(int2)), dz(zz.size() * sizeof(int2));
+  MVD_CHECK(cudaMemcpyAsync(dt.p, &t, sizeof(TileDesc), cudaMemcpyHostToDevice, s));
+  MVD_CHECK(cudaMemcpyAsync(df.p, fwd.data(), fwd.size() * sizeof(int2), cudaMemcpyHostToDevice, s));
+  MVD_CHECK(cudaMemcpyAsync(dz.p, zz.data(), zz.size() * sizeof(int2), cudaMemcpyHostToDevice, s));
+  GatherValue g{{scratch.as<float>(), tx, ty, tz}, 0.f};
+  launch_fwd_impl(pt, plan, dt.as<TileDesc>(), df.as<int2>(), (int)fwd.size(), plan.smem_plane, otf, g, s);
+  auto k = zpass_kernel<1>;
+  set_smem(k, plan.smem_z);
+  k<<<(int)zz.size(), kThreads, plan.smem_z, s>>>(dt.as<TileDesc>(), dz.as<int2>(), pt.device(), otf,
+                                                 nullptr, (float)(1.0 / ((double)tx * ty * tz)));
+  MVD_CHECK(cudaGetLastError());
+  // the temporary tables are freed when this returns: wait for the launches that read them
+  MVD_CHECK(cudaStreamSynchronize(s));
+}
+
+// ------------------------------------------------------------------------------------------
+// elementwise and reduction kernels
+// ------------------------------------------------------------------------------------------
+static int grid_for(long long n, int threads = 256) {
+  long long b = (n + threads - 1) / threads;
+  return (int)std::max<long long>(1, std::min<long long>(b, 152LL * 16));
+}
+
+__device__ __forceinline__ void block_reduce_add2(double a, double b, double* out) {
+  __shared__ double ra[32], rb[32];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    a += __shfl_xor_sync(0xffffffffu, a, o);
+    b += __shfl_xor_sync(0xffffffffu, b, o);
+  }
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (lane == 0) { ra[warp] = a; rb[warp] = b; }
+  __syncthreads();
+  if (warp == 0) {
+    const int nw = blockDim.x >> 5;
+    a = lane < nw ? ra[lane] : 0.0;
+    b = lane < nw ? rb[lane] : 0.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      a += __shfl_xor_sync(0xffffffffu, a, o);
+      b += __shfl_xor_sync(0xffffffffu, b, o);
+    }
+    if (lane == 0) {
+      atomicAdd(out, a);
+      atomicAdd(out + 1, b);
+    }
+  }
+}
+
+__global__ void sum_f64_kernel(const float* __restrict__ x, long long n, double* out) {
+  double a = 0.0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    a += (double)x[i];
+  __shared__ double r[32];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (lane == 0) r[warp] = a;
+  __syncthreads();
+  if (warp == 0) {
+    a = lane < (int)(blockDim.x >> 5) ? r[lane] : 0.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+    if (lane == 0) atomicAdd(out, a);
+  }
+}
+
+void dev_sum_f64(const float* x, long long n, double* out, cudaStream_t s) {
+  sum_f64_kernel<<<grid_for(n), 256, 0, s>>>(x, n, out);
+  MVD_CHECK(cudaGetLastError());
+}
+
+__global__ void scale_div_kernel(float* x, long long n, const double* d) {
+  const double div = *d;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    x[i] = (float)((double)x[i] / div);
+}
+
+void dev_scale_div(float* x, long long n, const double* d, cudaStream_t s) {
+  scale_div_kernel<<<grid_for(n), 256, 0, s>>>(x, n, d);
+  MVD_CHECK(cudaGetLastError());
+}
+
+// Mirror.mirror along every axis: p <-> n-1-p for p <= n/2 (for even n the middle pair is
+// swapped twice and stays in place: Mirror.java:94-112)
+__device__ __forceinline__ int mirror_pos(int p, int n) {
+  if ((n & 1) == 0 && (p == n / 2 - 1 || p == n / 2)) return p;
+  return n - 1 - p;
+}
+
+__global__ void mirror_kernel(const float* __restrict__ in, float* __restrict__ out, int nx, int ny, int nz) {
+  const long long n = (long long)nx * ny * nz;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const int x = (int)(i % nx);
+    const int y = (int)((i / nx) % ny);
+    const int z = (int)(i / ((long long)nx * ny));
+    out[i] = in[((long long)mirror_pos(z, nz) * ny + mirror_pos(y, ny)) * nx + mirror_pos(x, nx)];
+  }
+}
+
+void dev_mirror(const float* in, float* out, int nx, int ny, int nz, cudaStream_t s) {
+  mirror_kernel<<<grid_for((long long)nx * ny * nz), 256, 0, s>>>(in, out, nx, ny, nz);
+  MVD_CHECK(cudaGetLastError());
+}
+
+__global__ void mul_kernel(float* a, const float* b, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    a[i] = __fmul_rn(a[i], b[i]);
+}
+void dev_mul(float* a, const float* b, long long n, cudaStream_t s) {
+  mul_kernel<<<grid_for(n), 256, 0, s>>>(a, b, n);
+  MVD_CHECK(cudaGetLastError());
+}
+
+// MVDeconFFT.pow (:346-354): repeated float multiplication
+__global__ void pow_kernel(float* a, int power, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const float v = a[i];
+    float r = v;
+    for (int k = 1; k < power; ++k) r = __fmul_rn(r, v);
+    a[i] = r;
+  }
+}
+void dev_pow(float* a, int power, long long n, cudaStream_t s) {
+  pow_kernel<<<grid_for(n), 256, 0, s>>>(a, power, n);
+  MVD_CHECK(cudaGetLastError());
+}
+
+__global__ void fill_kernel(float* a, float v, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    a[i] = v;
+}
+void dev_fill(float* a, float v, long long n, cudaStream_t s) {
+  fill_kernel<<<grid_for(n), 256, 0, s>>>(a, v, n);
+  MVD_CHECK(cudaGetLastError());
+}
+
+struct ViewPtrs {
+  const float* p[16];
+};
+
+// FirstIteration.call (FirstIteration.java:84-154): per voxel the mean of the positive view
+// values; summed (FP64) over voxels with at least one positive value, and counted.
+__global__ void first_iteration_kernel(ViewPtrs v, int nviews, long long n, double* out) {
+  double sum = 0.0, cnt = 0.0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    double s = 0.0;
+    int c = 0;
+    for (int k = 0; k < nviews; ++k) {
+      const float x = __ldg(v.p[k] + i);
+      if (x > 0.f) { s += (double)x; ++c; }
+    }
+    if (c > 0) { sum += s / c; cnt += 1.0; }
+  }
+  block_reduce_add2(sum, cnt, out);
+}
+
+void dev_first_iteration(const float* const* views, int nviews, long long n, double* out, cudaStream_t s) {
+  ViewPtrs vp{};
+  if (nviews > 16) throw std::invalid_argument("at most 16 views");
+  for (int i = 0; i < nviews; ++i) vp.p[i] = views[i];
+  first_iteration_kernel<<<grid_for(n), 256, 0, s>>>(vp, nviews, n, out);
+  MVD_CHECK(cudaGetLastError());
+}
+
+// MVDeconvolution.java:133-147: psi := avg (0.5 if NaN)
+__global__ void fill_avg_kernel(float* psi, const double* sc, long long n) {
+  double avg = sc[0] / sc[1];
+  if (isnan(avg)) avg = 0.5;
+  const float v = (float)avg;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    psi[i] = v;
+}
+void dev_fill_from_avg(float* psi, const double* sc, long long n, cudaStream_t s) {
+  fill_avg_kernel<<<grid_for(n), 256, 0, s>>>(psi, sc, n);
+  MVD_CHECK(cudaGetLastError());
+}
+
+// MVDeconvolution.java:201-208: psi := 0 where no view has data
+__global__ void mask_kernel(float* psi, ViewPtrs v, int nviews, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    bool any = false;
+    for (int k = 0; k < nviews; ++k) any |= __ldg(v.p[k] + i) > 0.f;
+    if (!any) psi[i] = 0.f;
+  }
+}
+void dev_mask(float* psi, const float* const* views, int nviews, long long n, cudaStream_t s) {
+  ViewPtrs vp{};
+  if (nviews > 16) throw std::invalid_argument("at most 16 views");
+  for (int i = 0; i < nviews; ++i) vp.p[i] = views[i];
+  mask_kernel<<<grid_for(n), 256, 0, s>>>(psi, vp, nviews, n);
+  MVD_CHECK(cudaGetLastError());
+}
+
+__global__ void quotient_kernel(float* b, const float* img, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const float x = img[i];
+    b[i] = x > 0.f ? __fdiv_rn(x, b[i]) : 1.f;
+  }
+}
+void dev_quotient(float* b, const float* img, long long n, cudaStream_t s) {
+  quotient_kernel<<<grid_for(n), 256, 0, s>>>(b, img, n);
+  MVD_CHECK(cudaGetLastError());
+}
+
+__global__ void update_kernel(float* psi, const float* integral, const float* weight, float lambda, long long n,
+                              double* stat_sum, unsigned* stat_max) {
+  EpiUpdate e{psi, weight, lambda, stat_sum, stat_max, 0, 0, 0.f, 0.f};
+  e.acc_init();
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    e(i, integral[i]);
+  e.finish();
+}
+void dev_update(float* psi, const float* integral, const float* weight, float lambda, long long n,
+                double* stat_sum, unsigned* stat_max, cudaStream_t s) {
+  update_kernel<<<grid_for(n), 256, 0, s>>>(psi, integral, weight, lambda, n, stat_sum, stat_max);
+  MVD_CHECK(cudaGetLastError());
+}
+
+__global__ void copy_block_kernel(const float* __restrict__ vol, int nx, int ny, int nz, float* __restrict__ blk,
+                                  int bx, int by, int bz, int ox, int oy, int oz, int mode, float value) {
+  const long long n = (long long)bx * by * bz;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const int x = (int)(i % bx) + ox;
+    const int y = (int)((i / bx) % by) + oy;
+    const int z = (int)(i / ((long long)bx * by)) + oz;
+    float v;
+    if (mode == 0) {
+      v = vol[((long long)mirror_single(z, nz) * ny + mirror_single(y, ny)) * nx + mirror_single(x, nx)];
+    } else {
+      v = (x < 0 || y < 0 || z < 0 || x >= nx || y >= ny || z >= nz) ? value
+                                                                      : vol[((long long)z * ny + y) * nx + x];
+    }
+    blk[i] = v;
+  }
+}
+void dev_copy_block(const float* vol, int nx, int ny, int nz, float* block, int bx, int by, int bz, int ox,
+                    int oy, int oz, Ext ext, float value, cudaStream_t s) {
+  copy_block_kernel<<<grid_for((long long)bx * by * bz), 256, 0, s>>>(vol, nx, ny, nz, block, bx, by, bz, ox, oy,
+                                                                    oz, ext == Ext::Mirror ? 0 : 1, value);
+  MVD_CHECK(cudaGetLastError());
+}
+
+__global__ void paste_block_kernel(const float* __restrict__ blk, int bx, int by, int lx, int ly, int lz,
+                                   float* __restrict__ vol, int nx, int ny, int ex0, int ey0, int ez0, int sx,
+                                   int sy, int sz) {
+  const long long n = (long long)sx * sy * sz;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const int x = (int)(i % sx);
+    const int y = (int)((i / sx) % sy);
+    const int z = (int)(i / ((long long)sx * sy));
+    vol[((long long)(ez0 + z) * ny + (ey0 + y)) * nx + (ex0 + x)] =
+        blk[((long long)(lz + z) * by + (ly + y)) * bx + (lx + x)];
+  }
+}
+void dev_paste_block(const float* block, int bx, int by, int bz, int lx, int ly, int lz, float* vol, int nx,
+                     int ny, int nz, int ex0, int ey0, int ez0, int sx, int sy, int sz, cudaStream_t s) {
+  (void)bz;
+  (void)nz;
+  paste_block_kernel<<<grid_for((long long)sx * sy * sz), 256, 0, s>>>(block, bx, by, lx, ly, lz, vol, nx, ny, ex0,
+                                                                     ey0, ez0, sx, sy, sz);
+  MVD_CHECK(cudaGetLastError());
+}
+
+}  // namespace mvd

@@ -1,0 +1,137 @@
+// Host side of the tiled FFT convolution engine (internal C++ API; the C ABI is in capi.cu).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "kernels.cuh"
+
+namespace mvd {
+
+struct CudaError : std::runtime_error {
+  cudaError_t code;
+  CudaError(cudaError_t c, const std::string& what) : std::runtime_error(what), code(c) {}
+};
+
+void check_cuda(cudaError_t e, const char* what);
+#define MVD_CHECK(x) ::mvd::check_cuda((x), #x)
+
+// 2,3,5,7-smooth helpers
+bool is_smooth(int n);
+int next_smooth(int n, bool even);
+std::vector<int> factorize(int n);  // radices from {8,4,2,3,5,7}, product == n
+
+// Device memory owned by RAII
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  DevBuf() = default;
+  explicit DevBuf(size_t b) { alloc(b); }
+  ~DevBuf();
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  DevBuf(DevBuf&& o) noexcept : p(o.p), bytes(o.bytes) { o.p = nullptr; o.bytes = 0; }
+  DevBuf& operator=(DevBuf&& o) noexcept;
+  void alloc(size_t b);
+  void ensure(size_t b);  // grow (contents lost) if smaller
+  template <class T> T* as() const { return static_cast<T*>(p); }
+};
+
+// Twiddle tables and FFT plans for every length used on a device.
+class PlanTable {
+ public:
+  int index_of(int n);          // creates the plan if needed (host side only)
+  const FftPlan* device();      // uploads if changed; valid until the next upload
+  size_t size() const { return host_.size(); }
+ private:
+  static constexpr int kCapacity = 256;
+  std::vector<FftPlan> host_;
+  std::map<int, int> by_len_;
+  std::vector<std::unique_ptr<DevBuf>> tw_bufs_;
+  DevBuf dev_;
+  bool dirty_ = true;
+};
+
+// One axis of a tile grid.
+struct AxisTiles {
+  int size = 0, k = 0, T = 0, n = 0, E = 0;
+};
+
+// A convolution plan over one volume with one kernel size: the tiles, their work items and
+// the spectrum / OTF layout.
+struct ConvPlan {
+  int nx = 0, ny = 0, nz = 0;          // volume
+  int kx = 0, ky = 0, kz = 0;          // kernel
+  AxisTiles ax, ay, az;
+  std::vector<TileDesc> tiles;         // host copy
+  std::vector<int2> items_fwd, items_inv, items_z;
+  long long spec_elems = 0;            // complex elements of all tile spectra
+  long long otf_elems = 0;             // complex elements of one OTF (all tiles share the shape)
+  size_t smem_plane = 0, smem_z = 0;
+  DevBuf d_tiles, d_items_fwd, d_items_inv, d_items_z;
+  long long padded_voxels() const { return (long long)tiles.size() * ax.T * ay.T * az.T; }
+  void upload();
+};
+
+struct PlanOptions {
+  int force_tx = 0, force_ty = 0, force_tz = 0;  // 0 = planner's choice
+};
+
+// Choose tiles for a (volume, kernel) pair; effective regions cover the whole volume.
+std::unique_ptr<ConvPlan> make_conv_plan(PlanTable& pt, int nx, int ny, int nz, int kx, int ky,
+                                         int kz, const PlanOptions& opt = PlanOptions());
+
+// Describe the plan for logs.
+std::string describe(const ConvPlan& p);
+
+// Build the (scaled) spectrum of a kernel for the tile shape of `plan` into `otf`
+// (plan.otf_elems complex values).  `kernel` is a device [kz][ky][kx] float array.
+void build_otf(PlanTable& pt, const ConvPlan& plan, const float* kernel, float2* otf,
+               DevBuf& scratch_real, cudaStream_t s);
+
+enum class Ext { Mirror = 0, Value = 1 };
+
+// Full convolution out = ext(in) (*) kernel over the volume (out may alias nothing in `in`).
+void convolve(PlanTable& pt, const ConvPlan& plan, const float* in, Ext ext, float value,
+              const float2* otf, float2* spec, float* out, cudaStream_t s);
+
+// The three passes, for fused use by the deconvolution handle.
+void launch_fwd_mirror(PlanTable& pt, const ConvPlan& p, const float* vol, float2* spec, cudaStream_t s);
+void launch_fwd_value(PlanTable& pt, const ConvPlan& p, const float* vol, float value, float2* spec,
+                      cudaStream_t s);
+void launch_z(PlanTable& pt, const ConvPlan& p, float2* spec, const float2* otf, cudaStream_t s);
+void launch_inv_store(PlanTable& pt, const ConvPlan& p, const float2* spec, float* out, cudaStream_t s);
+void launch_inv_quotient(PlanTable& pt, const ConvPlan& p, const float2* spec, const float* img,
+                         float* q, cudaStream_t s);
+void launch_inv_update(PlanTable& pt, const ConvPlan& p, const float2* spec, float* psi,
+                       const float* weight, float lambda, double* stat_sum, unsigned* stat_max,
+                       cudaStream_t s);
+
+// ---- elementwise / reduction helpers (misc kernels) ----
+void dev_sum_f64(const float* x, long long n, double* out_dev, cudaStream_t s);  // *out += sum
+void dev_scale_div(float* x, long long n, const double* div_dev, cudaStream_t s); // x = (float)(x / d)
+void dev_mirror(const float* in, float* out, int nx, int ny, int nz, cudaStream_t s);
+void dev_mul(float* a, const float* b, long long n, cudaStream_t s);
+void dev_pow(float* a, int power, long long n, cudaStream_t s);
+void dev_fill(float* a, float v, long long n, cudaStream_t s);
+void dev_first_iteration(const float* const* views, int nviews, long long n, double* sum_count,
+                         cudaStream_t s);  // sum_count[0] += sum of means, [1] += count
+void dev_fill_from_avg(float* psi, const double* sum_count, long long n, cudaStream_t s);
+void dev_mask(float* psi, const float* const* views, int nviews, long long n, cudaStream_t s);
+void dev_quotient(float* blurred_to_q, const float* img, long long n, cudaStream_t s);
+void dev_update(float* psi, const float* integral, const float* weight, float lambda, long long n,
+                double* stat_sum, unsigned* stat_max, cudaStream_t s);
+// block copy / paste of the reference's Block.copyBlock / pasteBlock
+void dev_copy_block(const float* vol, int nx, int ny, int nz, float* block, int bx, int by, int bz,
+                    int ox, int oy, int oz, Ext ext, float value, cudaStream_t s);
+void dev_paste_block(const float* block, int bx, int by, int bz, int lx, int ly, int lz, float* vol,
+                     int nx, int ny, int nz, int ex0, int ey0, int ez0, int sx, int sy, int sz,
+                     cudaStream_t s);
+
+}  // namespace mvd

@@ -1,0 +1,131 @@
+"""Parity of the whole-deconvolution handle against the CPU oracle (GPU).
+
+The gate is the one the method states: relative L2 <= 1e-4 of psi against the FP64 oracle
+after the iterations run (the FP32 GPU path lands near 1e-6).  Kernel preparation, the
+first-iteration average, the per-view statistics and the masking are checked too.
+"""
+import numpy as np
+import pytest
+
+from oracle import mvdecon_oracle as O
+from spim_registration_gb300 import FLAG_NO_GRAPH, FLAG_PLAIN, PSFTYPE, Deconvolution, MVDeconFFT, MVDeconInput, \
+    MVDeconvolution
+from spim_registration_gb300 import synthetic as S
+from tests.helpers import rel_l2, rel_max
+
+pytestmark = pytest.mark.gpu
+
+RELL2 = 1e-4
+
+
+def small(cfg, ptype=None, it=4, shape=None, psf=None, views=None, lam=None):
+    defaults = {1: ((48, 40, 32), (7, 7, 13)), 2: ((64, 56, 48), (9, 9, 17)), 3: ((64, 64, 64), (9, 9, 17))}
+    sh, ps = defaults[cfg]
+    return S.make_problem(cfg, shape_xyz=shape or sh, psf_size_xyz=psf or ps, n_blobs=25, iterations=it,
+                          psftype=ptype, n_views=views, lam=lam)
+
+
+def run_gpu(p, flags=0, block=None, it=None):
+    d = Deconvolution(p.views, p.weights, p.psfs, p.psftype, p.lam, 0, flags, block)
+    d.run(p.iterations if it is None else it)
+    return d
+
+
+@pytest.mark.parametrize("cfg,ptype", [
+    (1, S.INDEPENDENT),
+    (2, S.EFFICIENT_BAYESIAN),
+    (2, S.OPTIMIZATION_I),
+    (2, S.OPTIMIZATION_II),
+    (3, S.EFFICIENT_BAYESIAN),
+])
+def test_deconvolution_matches_fp64_oracle(cfg, ptype):
+    p = small(cfg, ptype)
+    ref, od = O.deconvolve(p, arith="f64", block=None, mask=False)
+    d = run_gpu(p)
+    got = d.get_psi()
+    assert rel_l2(got, ref) < RELL2, rel_l2(got, ref)
+    # kernels of MVDeconFFT.init
+    for v in range(len(p.psfs)):
+        assert rel_max(d.kernel(v, 1), od.k1[v]) < 1e-6
+        assert rel_max(d.kernel(v, 2), od.k2[v]) < 1e-5
+    assert d.initial_average() == pytest.approx(od.avg, rel=1e-12)
+    # per-view statistics of the last iteration
+    last = p.iterations - 1
+    for v in range(len(p.psfs)):
+        s, m = d.stats(last, v)
+        _, _, rs, rm = [x for x in od.stats if x[0] == last and x[1] == v][0]
+        assert s == pytest.approx(rs, rel=1e-3)
+        assert m == pytest.approx(rm, rel=1e-3, abs=1e-6)
+
+
+def test_no_tikhonov_and_ten_iterations():
+    p = small(1, S.INDEPENDENT, it=10, lam=0.0)
+    ref, _ = O.deconvolve(p, arith="f64", block=None, mask=False)
+    got = run_gpu(p).get_psi()
+    assert rel_l2(got, ref) < RELL2
+
+
+def test_plain_blocked_form_matches_oracle_and_fused_form():
+    p = small(2, S.EFFICIENT_BAYESIAN, it=3)
+    ref, _ = O.deconvolve(p, arith="f64", block=(32, 32, 32), mask=False)
+    plain = run_gpu(p, FLAG_PLAIN, block=(32, 32, 32)).get_psi()
+    fused = run_gpu(p).get_psi()
+    assert rel_l2(plain, ref) < RELL2
+    assert rel_l2(fused, plain) < RELL2
+
+
+def test_plain_single_block_form():
+    p = small(1, S.INDEPENDENT, it=3)
+    ref, _ = O.deconvolve(p, arith="f64", block=None, mask=False)
+    got = run_gpu(p, FLAG_PLAIN, block=None).get_psi()
+    assert rel_l2(got, ref) < RELL2
+
+
+def test_graph_and_eager_and_per_view_calls_agree():
+    p = small(2, S.EFFICIENT_BAYESIAN, it=3)
+    a = run_gpu(p).get_psi()
+    b = run_gpu(p, FLAG_NO_GRAPH).get_psi()
+    d = Deconvolution(p.views, p.weights, p.psfs, p.psftype, p.lam, 0, 0)
+    for _ in range(p.iterations):
+        for v in range(len(p.views)):
+            d.run_view(v)
+    c = d.get_psi()
+    assert d.iteration() == p.iterations
+    np.testing.assert_array_equal(a, b)
+    np.testing.assert_array_equal(a, c)
+
+
+def test_mvdeconvolution_class_masks_and_matches():
+    p = small(3, S.EFFICIENT_BAYESIAN, it=3)  # cropped views: voxels without data exist
+    inp = MVDeconInput()
+    for img, w, k in zip(p.views, p.weights, p.psfs):
+        inp.add(MVDeconFFT(img, w, k, deviceList=[0]))
+    dec = MVDeconvolution(inp, PSFTYPE.EFFICIENT_BAYESIAN, p.iterations, p.lam, 1.0, 0, "test")
+    ref, _ = O.deconvolve(p, arith="f64", block=None, mask=True)
+    got = dec.getPsi()
+    nodata = np.all(np.stack(p.views) <= 0, axis=0)
+    assert nodata.any()
+    assert np.all(got[nodata] == 0)
+    assert rel_l2(got, ref) < RELL2
+
+
+def test_set_psi_checkpoint_resume():
+    p = small(1, S.INDEPENDENT, it=4)
+    full = run_gpu(p).get_psi()
+    d1 = run_gpu(p, it=2)
+    mid = d1.get_psi()
+    d2 = Deconvolution(p.views, p.weights, p.psfs, p.psftype, p.lam, 0, 0)
+    d2.set_psi(mid)
+    d2.run(2)
+    np.testing.assert_array_equal(d2.get_psi(), full)
+
+
+def test_single_view_and_invalid_arguments():
+    p = small(1, S.INDEPENDENT, it=2, views=1)
+    ref, _ = O.deconvolve(p, arith="f64", block=None, mask=False)
+    assert rel_l2(run_gpu(p).get_psi(), ref) < RELL2
+    from spim_registration_gb300.native import MvdError
+    with pytest.raises(MvdError):
+        Deconvolution(p.views, p.weights, [np.ones((4, 3, 3), np.float32)], p.psftype, p.lam)
+    with pytest.raises(MvdError):
+        Deconvolution(p.views, p.weights, p.psfs, 7, p.lam)

@@ -1,0 +1,161 @@
+"""Known-answer tests of the CPU oracle (no GPU).
+
+The reference ships no tests or golden vectors for this path, so the oracle is pinned by
+mathematical identities of the restated algorithm and by the committed golden fixtures that
+tests/golden/make_golden.py generates from it.
+"""
+import numpy as np
+import pytest
+
+from oracle import mvdecon_oracle as O
+from spim_registration_gb300 import synthetic as S
+
+
+def rng(seed=0):
+    return np.random.default_rng(seed)
+
+
+@pytest.mark.parametrize("mode,value", [(O.MIRROR, 0.0), (O.VALUE, 1.0), (O.VALUE, 0.0)])
+@pytest.mark.parametrize("shape,kshape", [((16, 16, 16), (5, 5, 9)), ((11, 7, 13), (3, 5, 7)), ((5, 6, 4), (7, 3, 9))])
+def test_fft_conv_equals_direct_conv(mode, value, shape, kshape):
+    r = rng(1)
+    img = r.random(shape)
+    k = r.random(kshape)
+    a = O.conv_extended(img, k, mode, value)
+    b = O.conv_direct(img, k, mode, value)
+    assert np.abs(a - b).max() < 1e-10 * max(1.0, np.abs(b).max())
+
+
+def test_delta_psf_is_identity():
+    img = rng(2).random((9, 10, 11))
+    k = np.zeros((5, 3, 7))
+    k[2, 1, 3] = 1.0
+    for mode in (O.MIRROR, O.VALUE):
+        np.testing.assert_allclose(O.conv_extended(img, k, mode, 1.0), img, atol=1e-12)
+
+
+def test_delta_image_gives_centred_psf():
+    img = np.zeros((21, 21, 21))
+    img[10, 10, 10] = 1.0
+    k = rng(3).random((5, 7, 9))
+    out = O.conv_extended(img, k, O.VALUE, 0.0)
+    np.testing.assert_allclose(out[8:13, 7:14, 6:15], k, atol=1e-12)
+    assert abs(out.sum() - k.sum()) < 1e-10
+
+
+def test_mirror_single_index_map():
+    n = 5
+    idx = np.arange(-6, 12)
+    m = O.mirror_single_index(idx, n)
+    # -1 -> 1, n -> n-2, period 2n-2
+    assert m[idx == -1][0] == 1 and m[idx == n][0] == n - 2
+    assert np.all((m >= 0) & (m < n))
+    assert np.array_equal(O.mirror_single_index(idx + 2 * n - 2, n), m)
+
+
+def test_mirror_kernel_odd_is_flip_even_keeps_middle():
+    a = np.arange(3 * 5 * 7, dtype=np.float64).reshape(3, 5, 7)
+    np.testing.assert_array_equal(O.mirror(a), a[::-1, ::-1, ::-1])
+    b = np.arange(4, dtype=np.float64).reshape(1, 1, 4)
+    # Mirror.java swaps p<->n-1-p for p <= n/2: the middle pair of an even axis is swapped twice
+    np.testing.assert_array_equal(O.mirror(b)[0, 0], [3, 1, 2, 0])
+
+
+def test_blocked_equals_single_block():
+    r = rng(4)
+    img = r.random((20, 23, 26))
+    k = r.random((7, 5, 9))
+    whole = O.conv_extended(img, k, O.MIRROR)
+    for block in [(12, 10, 14), (26, 23, 20), (9, 5, 7)]:
+        blk = O.convolve_blocked(img, k, block, O.MIRROR)
+        np.testing.assert_allclose(blk, whole, rtol=1e-12, atol=1e-12)
+    whole1 = O.conv_extended(img, k, O.VALUE, 1.0)
+    np.testing.assert_allclose(O.convolve_blocked(img, k, (12, 10, 14), O.VALUE, 1.0), whole1, rtol=1e-12, atol=1e-12)
+
+
+def test_block_generator_matches_reference_rules():
+    blocks = O.divide_into_blocks((100, 50, 30), (9, 9, 15), (32, 32, 32))
+    eff = (24, 24, 18)
+    assert len(blocks) == 5 * 3 * 2
+    covered = np.zeros((30, 50, 100), dtype=int)
+    for b in blocks:
+        for d in range(3):
+            assert b["offset"][d] == b["eff_offset"][d] - (9, 9, 15)[d] // 2
+            assert b["eff_size"][d] <= eff[d]
+        ex, ey, ez = b["eff_offset"]
+        sx, sy, sz = b["eff_size"]
+        covered[ez:ez + sz, ey:ey + sy, ex:ex + sx] += 1
+    assert np.all(covered == 1)
+    with pytest.raises(ValueError):
+        O.divide_into_blocks((10, 10, 10), (9, 9, 15), (8, 32, 32))
+
+
+def test_rl_fixed_point():
+    """img = psi (*) P, w = 1, lambda = 0: a view stage leaves psi unchanged."""
+    r = rng(5)
+    psi = 10 + 50 * r.random((12, 14, 16))
+    k = S.gaussian_psf((1.2, 1.0, 2.0), (5, 5, 9))
+    img = O.conv_extended(psi, k, O.MIRROR)
+    d = O.Deconvolution([img.astype(np.float32)], [np.ones_like(img, dtype=np.float32)], [k], O.INDEPENDENT, 0.0,
+                        psi0=psi)
+    # kernel2 = mirror(kernel1): the quotient is 1 everywhere, conv2 of 1 is 1 (value-1 border)
+    d.run_view(0)
+    np.testing.assert_allclose(d.psi, psi, rtol=1e-6)
+
+
+def test_normalisation_quirk_counts_portion_zero_twice():
+    k = np.ones((3, 3, 3), dtype=np.float32)
+    s = O.sum_img(k)
+    sq = O.sum_img(k, quirk_threads=2)  # 4 portions of 27 voxels: portion 0 has 6
+    assert s == 27 and sq == 33
+    assert abs(O.norm_img(k).sum() - 1) < 1e-12
+
+
+def test_compound_kernels_are_unit_sum_and_shaped():
+    psfs = [S.gaussian_psf((1.2, 1.2, 3.0), (7, 7, 11), a) for a in (0, 60, 120)]
+    for ptype in (O.EFFICIENT_BAYESIAN, O.OPTIMIZATION_I, O.OPTIMIZATION_II, O.INDEPENDENT):
+        k1, k2 = O.prepare_kernels(psfs, ptype)
+        for a, b, p in zip(k1, k2, psfs):
+            assert a.shape == p.shape and b.shape == p.shape
+            assert abs(b.sum() - 1) < 1e-9 and abs(a.sum() - 1) < 1e-9
+    # one view: every type reduces to the mirrored kernel (MVDeconFFT.java:197-201)
+    k1, k2 = O.prepare_kernels(psfs[:1], O.EFFICIENT_BAYESIAN)
+    np.testing.assert_allclose(k2[0], O.mirror(k1[0]))
+
+
+def test_first_iteration_average_and_mask():
+    a = np.array([[[0, 2, 4]]], dtype=np.float32)
+    b = np.array([[[0, 0, 6]]], dtype=np.float32)
+    avg, count = O.first_iteration([a, b])
+    assert avg == pytest.approx((2 + 5) / 2)
+    np.testing.assert_array_equal(count[0, 0], [0, 1, 2])
+
+
+def test_update_rules_match_java_float_semantics():
+    psi = np.array([1.0, 2.0, 0.5, 3.0], dtype=np.float32)
+    integral = np.array([2.0, 0.0, np.nan, 1.0], dtype=np.float32)
+    w = np.array([1.0, 1.0, 1.0, 0.5], dtype=np.float32)
+    new, s, m = O.compute_final_values(psi, integral, w, 0.006, "f32")
+    tik = lambda v: (np.sqrt(1 + 2 * 0.006 * v) - 1) / 0.006  # noqa: E731
+    assert new[0] == np.float32(tik(2.0))
+    f = np.float32
+    mv = f(1e-4)
+    # value 0 -> minValue, NaN -> minValue; then last + (next - last) * w in float
+    assert new[1] == f(f(2.0) + f(f(mv - f(2.0)) * f(1.0)))
+    assert new[2] == f(f(0.5) + f(f(mv - f(0.5)) * f(1.0)))
+    assert new[3] == np.float32(3.0 + (np.float32(tik(3.0)) - 3.0) * 0.5)
+    assert s == pytest.approx(float(np.abs(new - psi).astype(np.float64).sum()))
+
+
+def test_deconvolution_f32_tracks_f64():
+    p = S.make_problem(1, shape_xyz=(40, 36, 24), psf_size_xyz=(7, 7, 11), n_blobs=15, iterations=3)
+    a, _ = O.deconvolve(p, arith="f64")
+    b, _ = O.deconvolve(p, arith="f32")
+    assert np.linalg.norm(a - b) / np.linalg.norm(a) < 1e-5
+
+
+def test_blocked_deconvolution_equals_whole():
+    p = S.make_problem(2, shape_xyz=(40, 36, 28), psf_size_xyz=(5, 5, 9), n_blobs=15, iterations=2)
+    a, _ = O.deconvolve(p, block=None)
+    b, _ = O.deconvolve(p, block=(24, 20, 20))
+    np.testing.assert_allclose(a, b, rtol=1e-10, atol=1e-10)
