@@ -1,0 +1,397 @@
+"""Benchmark of the multiview deconvolution hot path: voxel-updates/s.
+
+One step = one deconvolution iteration (every view's conv1 -> quotient -> conv2 -> update) of
+the 4-view efficient-Bayesian workload 256x256x192, PSF 15x15x41 (sigma 1.5,1.5,5) rotated per
+view (0/45/90/135 deg about y), cosine-blended VIRTUAL weights; synthetic seeded inputs.
+voxel-updates/s = voxels * views * steps / time.
+
+Arms:
+  (default)          the sm_103a library: fused tiled passes, all tiles of a view in one launch
+                     per pass, one CUDA graph per iteration, inputs resident in HBM.
+  --impl reference   the reference algorithm on the host cores (the CPU restatement of the Java
+                     MVDeconvolution / MVDeconFFT path, float32, scipy FFT on every core); the
+                     reference's own Java code cannot run on this machine.
+
+Multi-GPU: the path does not shard across GPUs in this build (views are sequential, one GPU
+per box); with --gpus N each rank runs an independent replica on its own GPU ("weak" scaling,
+value = all ranks' voxel-updates / max time over ranks).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "voxel-updates/s, 4-view decon, batched+split vs plain FP32 form at relL2<=1e-4"
+
+WORKLOADS = {
+    # name: (cfg id, shape xyz, psf xyz, reference block for the plain form)
+    "cfg2_4view_eb_256x256x192": (2, (256, 256, 192), (15, 15, 41), (128, 128, 128)),
+    "cfg4_4view_eb_512x512x256": (4, (512, 512, 256), (31, 31, 61), None),
+    "cfg1_2view_128x128x64": (1, (128, 128, 64), (9, 9, 25), None),
+}
+DEFAULT_WORKLOAD = "cfg2_4view_eb_256x256x192"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS))
+    ap.add_argument("--no-plain", action="store_true", help="skip the plain FP32 form measurement")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return None
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(smax)), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def make_problem(workload):
+    from spim_registration_gb300 import synthetic as S
+
+    cfg, shape, psf, _ = WORKLOADS[workload]
+    return S.make_problem(cfg, shape_xyz=shape, psf_size_xyz=psf)
+
+
+def bytes_per_iteration(dec, n_views, n_voxels):
+    """Algorithmic HBM bytes of one fused iteration per pass kind (byte model)."""
+    out = {"plane_fwd": 0, "zpass": 0, "plane_inv_quotient": 0, "plane_inv_update": 0}
+    for v in range(n_views):
+        p = dec.plan(v)
+        tx, ty, tz = p["tile"]
+        ex, ey, ez = p["effective"]
+        nt = p["tiles"][0] * p["tiles"][1] * p["tiles"][2]
+        half = (tx // 2 + 1) * ty  # complex values per spectrum slice
+        P = nt * tx * ty * tz      # real voxels transformed
+        H = nt * half * tz         # complex values of the half spectrum
+        Heff = nt * half * min(ez, tz)
+        # forward plane: gather P reals, write H complex (x2 convolutions)
+        out["plane_fwd"] += 2 * (4 * P + 8 * H)
+        # z pass: read H, read OTF H, write H (x2)
+        out["zpass"] += 2 * (24 * H)
+        # inverse plane: read effective spectrum slices; quotient reads img, writes q
+        out["plane_inv_quotient"] += 8 * Heff + 8 * n_voxels
+        # update reads psi, weight, writes psi
+        out["plane_inv_update"] += 8 * Heff + 12 * n_voxels
+    return out
+
+
+def run_ours(args, rank, world, local):
+    import torch
+
+    from spim_registration_gb300 import FLAG_PLAIN, Deconvolution
+    from spim_registration_gb300 import native
+
+    torch.cuda.set_device(local)
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
+    peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
+
+    prob = make_problem(args.workload)
+    n_vox = prob.n_voxels
+    V = len(prob.views)
+    lib = native.load()
+
+    dec = Deconvolution(prob.views, prob.weights, prob.psfs, prob.psftype, prob.lam, local, 0)
+    stream = torch.cuda.ExternalStream(dec.stream(), device=local)
+
+    # warm-up (captures the graph on the first iteration)
+    for _ in range(args.warmup):
+        dec.run_iteration()
+    dec.synchronize()
+
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)  # let the sampler start before the timed region
+    launches0 = dec.launch_count()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        dec.run_iteration()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    clock_info = clocks.stop()
+    launches = dec.launch_count() - launches0
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([ms], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    ms_per_step = ms / args.steps
+    value = n_vox * V * args.steps * world / (ms / 1e3)
+
+    # per-pass device time (CUDA events on the library's stream) for the roofline
+    prof = dec.profile_iteration()
+    algo = bytes_per_iteration(dec, V, n_vox)
+    dom = max(("plane_fwd", "zpass", "plane_inv_quotient", "plane_inv_update"), key=lambda k: prof[k][0])
+    dom_ms, dom_launches = prof[dom]
+    achieved = algo[dom] / (dom_ms / 1e3) / 1e9
+    per_pass = {k: {"ms": round(prof[k][0], 4), "launches": prof[k][1],
+                    "gbs": round(algo[k] / (prof[k][0] / 1e3) / 1e9, 1) if k in algo and prof[k][0] > 0 else None}
+                for k in prof}
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tpath):
+        try:
+            traffic = json.load(open(tpath)).get(args.workload, {}).get(dom)
+        except Exception:
+            traffic = None
+
+    out = {
+        "metric": METRIC,
+        "value": value,
+        "unit": "voxel-updates/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms_per_step,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic (seeded blobs, Poisson noise, rotated Gaussian PSFs)",
+        "config": {"workload": args.workload, "views": V, "volume_xyz": list(prob.dims_xyz),
+                   "psf_xyz": [list(p.shape[::-1]) for p in prob.psfs], "psftype": "EFFICIENT_BAYESIAN",
+                   "lambda": prob.lam, "step": "one iteration over all views",
+                   "plans": [dec.plan(v) for v in range(V)],
+                   "l2": "working set per iteration > 129 MB L2 (no flush needed)",
+                   "parallelism": f"replicas x{world}"},
+        "gpu_launches": launches,
+        "clocks": clock_info,
+        "per_pass": per_pass,
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                     "frac": achieved / hbm_peak, "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)",
+                     "algorithmic_bytes_per_launch": algo[dom] / max(dom_launches, 1),
+                     "avg_launch_ms": dom_ms / max(dom_launches, 1), "traffic": traffic},
+    }
+    dec.close()
+
+    if rank == 0 and not args.no_plain:
+        # the plain FP32 form: reference block structure, one block per launch sequence
+        _, _, _, block = WORKLOADS[args.workload]
+        plain = Deconvolution(prob.views, prob.weights, prob.psfs, prob.psftype, prob.lam, local, FLAG_PLAIN, block)
+        pstream = torch.cuda.ExternalStream(plain.stream(), device=local)
+        plain.run_iteration()
+        plain.synchronize()
+        psteps = max(1, min(3, args.steps))
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        a.record(pstream)
+        for _ in range(psteps):
+            plain.run_iteration()
+        b.record(pstream)
+        torch.cuda.synchronize()
+        pms = a.elapsed_time(b) / psteps
+        pvalue = n_vox * V / (pms / 1e3)
+        # accuracy of the fused form against the plain form after the same iterations
+        fused = Deconvolution(prob.views, prob.weights, prob.psfs, prob.psftype, prob.lam, local, 0)
+        fused.run(1 + psteps)
+        f = fused.get_psi()
+        pl = plain.get_psi()
+        fused.close()
+        plain.close()
+        out["plain_fp32_form"] = {"value": pvalue, "ms_per_step": pms, "block_xyz": block,
+                                  "speedup_of_value": value / world / pvalue,
+                                  "rel_l2_fused_vs_plain": float(np.linalg.norm(f - pl) / np.linalg.norm(pl))}
+
+    if rank == 0 and not args.no_e2e:
+        out["e2e"] = run_e2e(prob, local, steps=2)
+    if rank == 0 and not args.no_cpu:
+        out["cpu_baseline"] = cpu_baseline(prob)
+    return out
+
+
+def run_e2e(prob, device, steps=2):
+    """Whole job through the C ABI with host buffers: upload (pinned), kernel preparation,
+    all iterations, masked psi back to the host."""
+    import torch
+
+    from spim_registration_gb300 import Deconvolution
+
+    def pinned(a):
+        t = torch.empty(a.shape, dtype=torch.float32, pin_memory=True)
+        t.numpy()[...] = a
+        return t.numpy()
+
+    views = [pinned(v) for v in prob.views]
+    weights = [pinned(w) for w in prob.weights]
+    psfs = [np.ascontiguousarray(p) for p in prob.psfs]
+    h2d = sum(v.nbytes for v in views) + sum(w.nbytes for w in weights) + sum(p.nbytes for p in psfs)
+    d2h = prob.views[0].nbytes
+    times = []
+    for i in range(steps + 1):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        d = Deconvolution(views, weights, psfs, prob.psftype, prob.lam, device, 0)
+        d.run(prob.iterations)
+        psi = d.get_psi(masked=True)
+        t1 = time.perf_counter()
+        d.close()
+        if i > 0:  # the first job pays the one-time CUDA context / module load
+            times.append(t1 - t0)
+        del psi
+    t = float(np.mean(times))
+    return {"value": prob.n_voxels * len(prob.views) * prob.iterations / t, "unit": "voxel-updates/s",
+            "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "seconds_per_job": t,
+            "step": f"one whole job: upload + kernel prep + {prob.iterations} iterations + masked psi download"}
+
+
+def cpu_view_stage_time(prob, workers=None):
+    """One view stage of the reference algorithm on the host cores (oracle port, float32)."""
+    from oracle import mvdecon_oracle as O
+
+    d = O.Deconvolution(prob.views, prob.weights, prob.psfs, prob.psftype, prob.lam, arith="f32")
+    d.run_view(0)  # warm (FFT plans, page-in)
+    t0 = time.perf_counter()
+    d.run_view(1 % len(prob.views))
+    return time.perf_counter() - t0
+
+
+def cpu_baseline(prob):
+    t = cpu_view_stage_time(prob)
+    return {"value": prob.n_voxels / t, "unit": "voxel-updates/s", "cores": os.cpu_count(), "kind": "port",
+            "sample": "one view stage (conv1, quotient, conv2, update) of the same workload, float32, "
+                      f"scipy.fft with {os.cpu_count()} workers; {t:.2f} s"}
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return None
+    prob = make_problem(args.workload)
+    from oracle import mvdecon_oracle as O
+
+    d = O.Deconvolution(prob.views, prob.weights, prob.psfs, prob.psftype, prob.lam, arith="f32")
+    V = len(prob.views)
+    for i in range(args.warmup):
+        d.run_view(i % V)
+    t0 = time.perf_counter()
+    for i in range(args.steps):
+        d.run_view(i % V)
+    t = time.perf_counter() - t0
+    value = prob.n_voxels * args.steps / t
+    return {
+        "impl": "reference",
+        "metric": METRIC,
+        "value": value,
+        "unit": "voxel-updates/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": t / args.steps * 1e3,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic (seeded blobs, Poisson noise, rotated Gaussian PSFs)",
+        "config": {"workload": args.workload, "views": V, "volume_xyz": list(prob.dims_xyz),
+                   "step": "one view stage (conv1, quotient, conv2, update) on the host cores"},
+        "cpu_baseline": {"value": value, "unit": "voxel-updates/s", "cores": os.cpu_count(), "kind": "port",
+                         "sample": f"{args.steps} view stages of the workload, CPU restatement of the Java "
+                                   "MVDeconvolution/MVDeconFFT loop (float32, scipy.fft on all cores); the Java "
+                                   "reference needs a JDK and its Maven jars, absent on this machine"},
+        "e2e": {"value": value, "unit": "voxel-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_env()
+    if args.steps > 0 and args.warmup < 0:
+        raise SystemExit("bad warmup")
+    if world > 1 and args.impl == "ours":
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    if args.impl == "reference":
+        out = run_reference(args, rank, world)
+    else:
+        out = run_ours(args, rank, world, local)
+    if rank == 0 and out is not None:
+        print(json.dumps(out))
+    if world > 1 and args.impl == "ours":
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

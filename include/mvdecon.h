@@ -127,6 +127,18 @@ int mvd_get_iteration(mvd_decon* h, int* iteration);
 int mvd_get_plan(mvd_decon* h, int view, int* tiles_xyz, int* tile_xyz, int* eff_xyz,
                  long long* padded_voxels);
 
+/* The cudaStream_t the handle enqueues on (for events recorded by the caller). */
+int mvd_get_stream(mvd_decon* h, void** stream);
+
+/* Kernel launches the handle has issued so far (graph replays count every node). */
+int mvd_get_launch_count(mvd_decon* h, long long* launches);
+
+/* Runs one iteration eagerly with CUDA events around each pass and returns the summed
+ * device time per pass kind in milliseconds: ms[0] forward plane passes, ms[1] z passes,
+ * ms[2] inverse plane + quotient, ms[3] inverse plane + update, ms[4] everything else;
+ * launches[k] the number of launches of each kind. */
+int mvd_profile_iteration(mvd_decon* h, double* ms, int* launches);
+
 #ifdef __cplusplus
 }
 #endif

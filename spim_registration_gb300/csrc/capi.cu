@@ -335,6 +335,8 @@ struct mvd_decon {
   int iteration = 0;
   double avg = 0.0;
   cudaGraphExec_t graph = nullptr;
+  long long graph_kernels = 0;  // kernel launches one replay of the graph performs
+  long long launches = 0;       // kernel launches issued by this handle
 
   ~mvd_decon() {
     if (graph) cudaGraphExecDestroy(graph);
@@ -360,6 +362,7 @@ struct mvd_decon {
     }
     archive_stats_kernel<<<1, 1, 0, s>>>(slot(v), hist.as<double>(), d_iter.as<int>(), v, V);
     MVD_CHECK(cudaGetLastError());
+    count_launch();
   }
 
   // one block per launch sequence: copy block -> 3 FFT passes -> paste (MVDeconFFT.java:438-446,
@@ -388,6 +391,7 @@ struct mvd_decon {
     for (int v = 0; v < V; ++v) enqueue_view(v);
     advance_iter_kernel<<<1, 1, 0, stream>>>(d_iter.as<int>());
     MVD_CHECK(cudaGetLastError());
+    count_launch();
   }
 
   void run_iteration() {
@@ -397,6 +401,7 @@ struct mvd_decon {
         pt.device();  // no synchronous uploads may happen during capture
         cudaGraph_t g = nullptr;
         MVD_CHECK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+        const long long before = launch_count();
         try {
           enqueue_iteration();
         } catch (...) {
@@ -405,13 +410,17 @@ struct mvd_decon {
           throw;
         }
         MVD_CHECK(cudaStreamEndCapture(stream, &g));
+        graph_kernels = launch_count() - before;
         cudaError_t e = cudaGraphInstantiate(&graph, g, 0);
         cudaGraphDestroy(g);
         MVD_CHECK(e);
       }
       MVD_CHECK(cudaGraphLaunch(graph, stream));
+      launches += graph_kernels;
     } else {
+      const long long before = launch_count();
       enqueue_iteration();
+      launches += launch_count() - before;
     }
     ++iteration;
   }
@@ -623,6 +632,7 @@ extern "C" int mvd_run_view(mvd_decon* h, int view) {
   if (view == h->V - 1) {
     advance_iter_kernel<<<1, 1, 0, h->stream>>>(h->d_iter.as<int>());
     MVD_CHECK(cudaGetLastError());
+    count_launch();
     ++h->iteration;
   }
   return MVD_OK;
@@ -746,4 +756,77 @@ extern "C" int mvd_get_plan(mvd_decon* h, int view, int* tiles, int* tile, int* 
     *padded = pv;
   }
   return MVD_OK;
+}
+
+extern "C" int mvd_get_stream(mvd_decon* h, void** stream) {
+  if (!h || !stream) return fail(MVD_ERR_ARG, "NULL argument");
+  *stream = (void*)h->stream;
+  return MVD_OK;
+}
+
+extern "C" int mvd_get_launch_count(mvd_decon* h, long long* launches) {
+  if (!h || !launches) return fail(MVD_ERR_ARG, "NULL argument");
+  *launches = h->launches;
+  return MVD_OK;
+}
+
+extern "C" int mvd_profile_iteration(mvd_decon* h, double* ms, int* launches) {
+  MVD_API_BEGIN
+  if (!h || !ms || !launches) return fail(MVD_ERR_ARG, "NULL argument");
+  if (h->flags & MVD_FLAG_PLAIN) return fail(MVD_ERR_STATE, "pass profiling needs the fused form");
+  MVD_CHECK(cudaSetDevice(h->dev));
+  cudaStream_t s = h->stream;
+  const int kinds = 5;
+  std::vector<cudaEvent_t> ev;
+  std::vector<int> kind;
+  auto mark = [&](int k) {
+    cudaEvent_t e;
+    MVD_CHECK(cudaEventCreate(&e));
+    MVD_CHECK(cudaEventRecord(e, s));
+    ev.push_back(e);
+    kind.push_back(k);
+  };
+  for (int k = 0; k < kinds; ++k) {
+    ms[k] = 0.0;
+    launches[k] = 0;
+  }
+  mark(-1);
+  for (int v = 0; v < h->V; ++v) {
+    const ConvPlan& p = *h->plans[v];
+    float2* sp = h->spec.as<float2>();
+    MVD_CHECK(cudaMemsetAsync(h->slot(v), 0, sizeof(StatSlot), s));
+    mark(4);
+    launch_fwd_mirror(h->pt, p, h->psi.as<float>(), sp, s);
+    mark(0);
+    launch_z(h->pt, p, sp, h->otf1[v].as<float2>(), s);
+    mark(1);
+    launch_inv_quotient(h->pt, p, sp, h->img[v].as<float>(), h->q.as<float>(), s);
+    mark(2);
+    launch_fwd_value(h->pt, p, h->q.as<float>(), 1.f, sp, s);
+    mark(0);
+    launch_z(h->pt, p, sp, h->otf2[v].as<float2>(), s);
+    mark(1);
+    launch_inv_update(h->pt, p, sp, h->psi.as<float>(), h->w[v].as<float>(), h->lambda, &h->slot(v)->sum,
+                      &h->slot(v)->max_bits, s);
+    mark(3);
+    archive_stats_kernel<<<1, 1, 0, s>>>(h->slot(v), h->hist.as<double>(), h->d_iter.as<int>(), v, h->V);
+    MVD_CHECK(cudaGetLastError());
+    mark(4);
+  }
+  advance_iter_kernel<<<1, 1, 0, s>>>(h->d_iter.as<int>());
+  MVD_CHECK(cudaGetLastError());
+  mark(4);
+  MVD_CHECK(cudaStreamSynchronize(s));
+  for (size_t i = 1; i < ev.size(); ++i) {
+    float t = 0.f;
+    MVD_CHECK(cudaEventElapsedTime(&t, ev[i - 1], ev[i]));
+    ms[kind[i]] += t;
+    launches[kind[i]] += 1;
+  }
+  launches[4] = h->V + 1;  // archive kernels + the iteration counter
+  for (auto e : ev) cudaEventDestroy(e);
+  ++h->iteration;
+  h->launches += 6 * h->V + h->V + 1;
+  return MVD_OK;
+  MVD_API_END
 }

@@ -1,6 +1,7 @@
 // Host engine of the tiled FFT convolution: plans, tile planner, OTF preparation, launches,
 // and the small elementwise / reduction kernels of the deconvolution path.
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <sstream>
@@ -8,6 +9,10 @@
 #include "engine.h"
 
 namespace mvd {
+
+static std::atomic<long long> g_launches{0};
+long long launch_count() { return g_launches.load(); }
+void count_launch(int n) { g_launches += n; }
 
 void check_cuda(cudaError_t e, const char* what) {
   if (e != cudaSuccess) {
@@ -281,6 +286,7 @@ static void launch_fwd_impl(PlanTable& pt, const ConvPlan& p, const TileDesc* ti
   set_smem(k, smem);
   k<<<nitems, kThreads, smem, s>>>(tiles, items, pt.device(), spec, g);
   MVD_CHECK(cudaGetLastError());
+  count_launch();
 }
 
 template <class Epi>
@@ -291,6 +297,7 @@ static void launch_inv_impl(PlanTable& pt, const ConvPlan& p, const float2* spec
   k<<<(int)p.items_inv.size(), kThreads, p.smem_plane, s>>>(p.d_tiles.as<TileDesc>(),
                                                              p.d_items_inv.as<int2>(), pt.device(), spec, e);
   MVD_CHECK(cudaGetLastError());
+  count_launch();
 }
 
 void launch_fwd_mirror(PlanTable& pt, const ConvPlan& p, const float* vol, float2* spec, cudaStream_t s) {
@@ -313,6 +320,7 @@ void launch_z(PlanTable& pt, const ConvPlan& p, float2* spec, const float2* otf,
   k<<<(int)p.items_z.size(), kThreads, p.smem_z, s>>>(p.d_tiles.as<TileDesc>(), p.d_items_z.as<int2>(),
                                                        pt.device(), spec, otf, 1.f);
   MVD_CHECK(cudaGetLastError());
+  count_launch();
 }
 
 void launch_inv_store(PlanTable& pt, const ConvPlan& p, const float2* spec, float* out, cudaStream_t s) {
@@ -372,6 +380,7 @@ void build_otf(PlanTable& pt, const ConvPlan& plan, const float* kernel, float2*
   place_kernel_kernel<<<(int)std::min<long long>((kn + 255) / 256, 4096), 256, 0, s>>>(
       kernel, plan.kx, plan.ky, plan.kz, scratch.as<float>(), tx, ty, tz);
   MVD_CHECK(cudaGetLastError());
+  count_launch();
   // one tile covering the placed kernel volume exactly; its spectrum goes to `otf`
   TileDesc t = plan.tiles[0];
   t.ox = t.oy = t.oz = 0;
@@ -393,6 +402,7 @@ void build_otf(PlanTable& pt, const ConvPlan& plan, const float* kernel, float2*
   k<<<(int)zz.size(), kThreads, plan.smem_z, s>>>(dt.as<TileDesc>(), dz.as<int2>(), pt.device(), otf,
                                                  nullptr, (float)(1.0 / ((double)tx * ty * tz)));
   MVD_CHECK(cudaGetLastError());
+  count_launch();
   // the temporary tables are freed when this returns: wait for the launches that read them
   MVD_CHECK(cudaStreamSynchronize(s));
 }
@@ -452,6 +462,7 @@ __global__ void sum_f64_kernel(const float* __restrict__ x, long long n, double*
 void dev_sum_f64(const float* x, long long n, double* out, cudaStream_t s) {
   sum_f64_kernel<<<grid_for(n), 256, 0, s>>>(x, n, out);
   MVD_CHECK(cudaGetLastError());
+  count_launch();
 }
 
 __global__ void scale_div_kernel(float* x, long long n, const double* d) {
@@ -463,6 +474,7 @@ __global__ void scale_div_kernel(float* x, long long n, const double* d) {
 void dev_scale_div(float* x, long long n, const double* d, cudaStream_t s) {
   scale_div_kernel<<<grid_for(n), 256, 0, s>>>(x, n, d);
   MVD_CHECK(cudaGetLastError());
+  count_launch();
 }
 
 // Mirror.mirror along every axis: p <-> n-1-p for p <= n/2 (for even n the middle pair is
@@ -485,6 +497,7 @@ __global__ void mirror_kernel(const float* __restrict__ in, float* __restrict__ 
 void dev_mirror(const float* in, float* out, int nx, int ny, int nz, cudaStream_t s) {
   mirror_kernel<<<grid_for((long long)nx * ny * nz), 256, 0, s>>>(in, out, nx, ny, nz);
   MVD_CHECK(cudaGetLastError());
+  count_launch();
 }
 
 __global__ void mul_kernel(float* a, const float* b, long long n) {
@@ -494,6 +507,7 @@ __global__ void mul_kernel(float* a, const float* b, long long n) {
 void dev_mul(float* a, const float* b, long long n, cudaStream_t s) {
   mul_kernel<<<grid_for(n), 256, 0, s>>>(a, b, n);
   MVD_CHECK(cudaGetLastError());
+  count_launch();
 }
 
 // MVDeconFFT.pow (:346-354): repeated float multiplication
@@ -508,6 +522,7 @@ __global__ void pow_kernel(float* a, int power, long long n) {
 void dev_pow(float* a, int power, long long n, cudaStream_t s) {
   pow_kernel<<<grid_for(n), 256, 0, s>>>(a, power, n);
   MVD_CHECK(cudaGetLastError());
+  count_launch();
 }
 
 __global__ void fill_kernel(float* a, float v, long long n) {
@@ -517,6 +532,7 @@ __global__ void fill_kernel(float* a, float v, long long n) {
 void dev_fill(float* a, float v, long long n, cudaStream_t s) {
   fill_kernel<<<grid_for(n), 256, 0, s>>>(a, v, n);
   MVD_CHECK(cudaGetLastError());
+  count_launch();
 }
 
 struct ViewPtrs {
@@ -545,6 +561,7 @@ void dev_first_iteration(const float* const* views, int nviews, long long n, dou
   for (int i = 0; i < nviews; ++i) vp.p[i] = views[i];
   first_iteration_kernel<<<grid_for(n), 256, 0, s>>>(vp, nviews, n, out);
   MVD_CHECK(cudaGetLastError());
+  count_launch();
 }
 
 // MVDeconvolution.java:133-147: psi := avg (0.5 if NaN)
@@ -558,6 +575,7 @@ __global__ void fill_avg_kernel(float* psi, const double* sc, long long n) {
 void dev_fill_from_avg(float* psi, const double* sc, long long n, cudaStream_t s) {
   fill_avg_kernel<<<grid_for(n), 256, 0, s>>>(psi, sc, n);
   MVD_CHECK(cudaGetLastError());
+  count_launch();
 }
 
 // MVDeconvolution.java:201-208: psi := 0 where no view has data
@@ -574,6 +592,7 @@ void dev_mask(float* psi, const float* const* views, int nviews, long long n, cu
   for (int i = 0; i < nviews; ++i) vp.p[i] = views[i];
   mask_kernel<<<grid_for(n), 256, 0, s>>>(psi, vp, nviews, n);
   MVD_CHECK(cudaGetLastError());
+  count_launch();
 }
 
 __global__ void quotient_kernel(float* b, const float* img, long long n) {
@@ -585,6 +604,7 @@ __global__ void quotient_kernel(float* b, const float* img, long long n) {
 void dev_quotient(float* b, const float* img, long long n, cudaStream_t s) {
   quotient_kernel<<<grid_for(n), 256, 0, s>>>(b, img, n);
   MVD_CHECK(cudaGetLastError());
+  count_launch();
 }
 
 __global__ void update_kernel(float* psi, const float* integral, const float* weight, float lambda, long long n,
@@ -599,6 +619,7 @@ void dev_update(float* psi, const float* integral, const float* weight, float la
                 double* stat_sum, unsigned* stat_max, cudaStream_t s) {
   update_kernel<<<grid_for(n), 256, 0, s>>>(psi, integral, weight, lambda, n, stat_sum, stat_max);
   MVD_CHECK(cudaGetLastError());
+  count_launch();
 }
 
 __global__ void copy_block_kernel(const float* __restrict__ vol, int nx, int ny, int nz, float* __restrict__ blk,
@@ -623,6 +644,7 @@ void dev_copy_block(const float* vol, int nx, int ny, int nz, float* block, int 
   copy_block_kernel<<<grid_for((long long)bx * by * bz), 256, 0, s>>>(vol, nx, ny, nz, block, bx, by, bz, ox, oy,
                                                                     oz, ext == Ext::Mirror ? 0 : 1, value);
   MVD_CHECK(cudaGetLastError());
+  count_launch();
 }
 
 __global__ void paste_block_kernel(const float* __restrict__ blk, int bx, int by, int lx, int ly, int lz,
@@ -644,6 +666,7 @@ void dev_paste_block(const float* block, int bx, int by, int bz, int lx, int ly,
   paste_block_kernel<<<grid_for((long long)sx * sy * sz), 256, 0, s>>>(block, bx, by, lx, ly, lz, vol, nx, ny, ex0,
                                                                      ey0, ez0, sx, sy, sz);
   MVD_CHECK(cudaGetLastError());
+  count_launch();
 }
 
 }  // namespace mvd

@@ -113,6 +113,10 @@ void launch_inv_update(PlanTable& pt, const ConvPlan& p, const float2* spec, flo
                        const float* weight, float lambda, double* stat_sum, unsigned* stat_max,
                        cudaStream_t s);
 
+// Kernel launches issued by this library (all devices), for launch accounting.
+long long launch_count();
+void count_launch(int n = 1);
+
 // ---- elementwise / reduction helpers (misc kernels) ----
 void dev_sum_f64(const float* x, long long n, double* out_dev, cudaStream_t s);  // *out += sum
 void dev_scale_div(float* x, long long n, const double* div_dev, cudaStream_t s); // x = (float)(x / d)

@@ -211,6 +211,25 @@ class Deconvolution:
         native.check(self.lib.mvd_get_iteration(self.h, ctypes.byref(i)))
         return i.value
 
+    def stream(self) -> int:
+        """cudaStream_t (as an integer) the handle enqueues on."""
+        v = ctypes.c_void_p()
+        native.check(self.lib.mvd_get_stream(self.h, ctypes.byref(v)))
+        return int(v.value or 0)
+
+    def launch_count(self) -> int:
+        n = ctypes.c_longlong()
+        native.check(self.lib.mvd_get_launch_count(self.h, ctypes.byref(n)))
+        return n.value
+
+    def profile_iteration(self):
+        """One eager iteration with per-pass CUDA events: {kind: (ms, launches)}."""
+        ms = (ctypes.c_double * 5)()
+        ln = (ctypes.c_int * 5)()
+        native.check(self.lib.mvd_profile_iteration(self.h, ms, ln))
+        names = ["plane_fwd", "zpass", "plane_inv_quotient", "plane_inv_update", "other"]
+        return {n: (ms[i], ln[i]) for i, n in enumerate(names)}
+
     def plan(self, view: int):
         t, s, e = (ctypes.c_int * 3)(), (ctypes.c_int * 3)(), (ctypes.c_int * 3)()
         pv = ctypes.c_longlong()

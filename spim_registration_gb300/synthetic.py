@@ -147,8 +147,8 @@ def blur_mirror(vol: np.ndarray, psf: np.ndarray) -> np.ndarray:
         )
     ].astype(np.float64)
     shape = [ext.shape[i] + psf.shape[i] - 1 for i in range(3)]
-    f = np.fft.rfftn(ext, shape) * np.fft.rfftn(psf.astype(np.float64), shape)
-    full = np.fft.irfftn(f, shape)
+    f = np.fft.rfftn(ext, shape, axes=(0, 1, 2)) * np.fft.rfftn(psf.astype(np.float64), shape, axes=(0, 1, 2))
+    full = np.fft.irfftn(f, shape, axes=(0, 1, 2))
     return full[kz - 1 : kz - 1 + nz, ky - 1 : ky - 1 + ny, kx - 1 : kx - 1 + nx]
 
 
@@ -269,7 +269,9 @@ def make_problem(
         coverage = []
         for _ in cfg["angles"]:
             m = np.zeros(shape_zyx, dtype=bool)
-            side = [int(rng.integers(min(96, s), s + 1)) for s in (nx, ny, nz)]
+            # sides U[96, 256] on a 256 box; the same fractions on a shrunk box
+            side = [int(rng.integers(max(4, (96 * s) // 256), max(5, (256 * s) // 256) + 1)) for s in (nx, ny, nz)]
+            side = [min(sd, s) for sd, s in zip(side, (nx, ny, nz))]
             off = [int(rng.integers(0, s - sd + 1)) for s, sd in zip((nx, ny, nz), side)]
             m[off[2]:off[2] + side[2], off[1]:off[1] + side[1], off[0]:off[0] + side[0]] = True
             coverage.append(m)
