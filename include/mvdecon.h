@@ -86,6 +86,19 @@ int mvd_convolve3d_device(const float* in, float* out, const int* dims_xyz, cons
                           const int* kdims_xyz, int ext_mode, float ext_value, int devCUDA,
                           void* stream);
 
+/* No counterpart in the reference.  mvd_convolve3d_device without any device allocation, for
+ * callers that may not call cudaMalloc / cudaFree while they run (a streaming acquisition
+ * pipeline that cannot take an allocation's device-wide synchronisation, or a host framework
+ * whose memory manager owns the device pool).  Same arguments and result as
+ * mvd_convolve3d_device; all working memory comes from one static 64 MiB device array per GPU
+ * (held until the process exits), and sizes whose plans, spectra and tables do not fit it are
+ * rejected with MVD_ERR_ARG and a message.  The first call on a device looks the array up
+ * (make it before any stream capture).  Calls share the array: calls that overlap on the GPU
+ * race and must be serialised by the caller.  Returns after enqueueing on `stream`. */
+int mvd_convolve3d_device_noalloc(const float* in, float* out, const int* dims_xyz, const float* kernel,
+                                  const int* kdims_xyz, int ext_mode, float ext_value, int devCUDA,
+                                  void* stream);
+
 /* ----- whole-deconvolution handle: MVDeconvolution / MVDeconInput / MVDeconFFT -----
  * (spim/process/fusion/deconvolution/MVDeconvolution.java:94-211, MVDeconFFT.java:79-324)
  * mvd_create uploads the views, weights and PSFs, prepares kernel1/kernel2 per PSFTYPE

@@ -136,6 +136,10 @@ void check_dims(const int* d, const char* what) {
 
 }  // namespace
 
+namespace mvd {
+void set_last_error(const std::string& msg) { g_last_error = msg; }
+}  // namespace mvd
+
 // =========================================================================================
 // Part 1: JNA interface
 // =========================================================================================

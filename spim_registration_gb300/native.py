@@ -50,6 +50,8 @@ SIGNATURES = {
     "mvd_convolve3d_inplace": (ctypes.c_int, [_F, _I, _F, _I, ctypes.c_int]),
     "mvd_convolve3d_device": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, _I, ctypes.c_void_p, _I,
                                              ctypes.c_int, ctypes.c_float, ctypes.c_int, ctypes.c_void_p]),
+    "mvd_convolve3d_device_noalloc": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, _I, ctypes.c_void_p, _I,
+                                                     ctypes.c_int, ctypes.c_float, ctypes.c_int, ctypes.c_void_p]),
     "mvd_create": (ctypes.c_int, [ctypes.POINTER(_H), ctypes.c_int, _I, ctypes.c_int, ctypes.POINTER(_F),
                                   ctypes.POINTER(_F), ctypes.POINTER(_F), _I, ctypes.c_int, ctypes.c_double,
                                   ctypes.c_int, _I]),
