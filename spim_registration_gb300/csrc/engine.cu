@@ -61,16 +61,32 @@ int next_smooth(int n, bool even) {
   }
 }
 
+// Radices of the register DFTs (fft_device.cuh).
+static const int kRadices[] = {16, 15, 14, 12, 10, 9, 8, 7, 6, 5, 4, 3, 2};
+
+static void best_split(int n, int depth, int maxdepth, std::vector<int>& cur, std::vector<int>& best) {
+  if (n == 1) {
+    // fewest stages first, then the most balanced (largest smallest radix)
+    auto mn = [](const std::vector<int>& v) { return v.empty() ? 0 : *std::min_element(v.begin(), v.end()); };
+    if (best.empty() || cur.size() < best.size() || (cur.size() == best.size() && mn(cur) > mn(best))) best = cur;
+    return;
+  }
+  if (depth == maxdepth) return;
+  for (int r : kRadices) {
+    if (n % r) continue;
+    if (!cur.empty() && r > cur.back()) continue;  // non-increasing order
+    cur.push_back(r);
+    best_split(n / r, depth + 1, maxdepth, cur, best);
+    cur.pop_back();
+  }
+}
+
 std::vector<int> factorize(int n) {
-  std::vector<int> r;
-  while (n % 8 == 0) { r.push_back(8); n /= 8; }
-  if (n % 4 == 0) { r.push_back(4); n /= 4; }
-  if (n % 2 == 0) { r.push_back(2); n /= 2; }
-  for (int f : {7, 5, 3})
-    while (n % f == 0) { r.push_back(f); n /= f; }
-  if (n != 1) throw std::invalid_argument("FFT length is not 2,3,5,7-smooth");
-  if (r.empty()) r.push_back(1);
-  return r;
+  if (n == 1) return {1};
+  std::vector<int> cur, best;
+  for (int depth = 1; depth <= kMaxStages && best.empty(); ++depth) best_split(n, 0, depth, cur, best);
+  if (best.empty()) throw std::invalid_argument("FFT length is not 2,3,5,7-smooth");
+  return best;
 }
 
 // ------------------------------------------------------------------------------------------
@@ -83,7 +99,7 @@ int PlanTable::index_of(int n) {
   if ((int)host_.size() >= kCapacity) throw std::runtime_error("FFT plan table full");
   FftPlan p{};
   p.n = n;
-  std::vector<int> rad = (n == 1) ? std::vector<int>{} : factorize(n);
+  std::vector<int> rad = factorize(n);
   if ((int)rad.size() > kMaxStages) throw std::invalid_argument("too many FFT stages");
   p.nstages = (int)rad.size();
   for (size_t i = 0; i < rad.size(); ++i) p.radix[i] = rad[i];
@@ -196,8 +212,7 @@ std::unique_ptr<ConvPlan> make_conv_plan(PlanTable& pt, int nx, int ny, int nz, 
   AxisTiles bx, by, bz;
   for (auto& a : ox)
     for (auto& b : oy) {
-      const int pxa = a.T / 2 + 1;
-      if ((long long)((pxa & 1) ? pxa : pxa + 1) * b.T > kPlaneCap) continue;
+      if ((long long)row_pitch(a.T / 2) * b.T > kPlaneCap) continue;
       for (auto& c : oz) {
         const double ntiles = (double)a.n * b.n * c.n;
         const double cost = ntiles * a.T * b.T * c.T * (1.0 + 1e-3 * ntiles);
@@ -216,7 +231,7 @@ std::unique_ptr<ConvPlan> make_conv_plan(PlanTable& pt, int nx, int ny, int nz, 
   p.kx = kx; p.ky = ky; p.kz = kz;
   p.ax = bx; p.ay = by; p.az = bz;
   const int px = bx.T / 2 + 1;
-  const int pitch = (px & 1) ? px : px + 1;
+  const int pitch = row_pitch(bx.T / 2);
   const int plx = pt.index_of(bx.T / 2), ply = pt.index_of(by.T), plz = pt.index_of(bz.T);
   const long long tile_spec = (long long)px * by.T * bz.T;
   long long off = 0;
@@ -258,10 +273,10 @@ std::string describe(const ConvPlan& p) {
 }
 
 // ------------------------------------------------------------------------------------------
-// launches
+// launches (the pass kernels are instantiated in passes_fwd.cu, passes_inv.cu, passes_z.cu)
 // ------------------------------------------------------------------------------------------
 // raise a kernel's dynamic shared-memory limit once per (device, kernel, size)
-static void set_smem_raw(const void* kernel, size_t bytes) {
+void set_smem_raw(const void* kernel, size_t bytes) {
   static std::mutex mu;
   static std::map<std::pair<int, const void*>, size_t> done;
   int dev = 0;
@@ -272,73 +287,6 @@ static void set_smem_raw(const void* kernel, size_t bytes) {
   if (it != done.end() && it->second >= bytes) return;
   MVD_CHECK(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
   done[key] = bytes;
-}
-template <class K>
-static void set_smem(K kernel, size_t bytes) {
-  set_smem_raw(reinterpret_cast<const void*>(kernel), bytes);
-}
-
-template <class Gather>
-static void launch_fwd_impl(PlanTable& pt, const ConvPlan& p, const TileDesc* tiles, const int2* items,
-                            int nitems, size_t smem, float2* spec, Gather g, cudaStream_t s) {
-  if (nitems == 0) return;
-  auto k = plane_fwd_kernel<Gather>;
-  set_smem(k, smem);
-  k<<<nitems, kThreads, smem, s>>>(tiles, items, pt.device(), spec, g);
-  MVD_CHECK(cudaGetLastError());
-  count_launch();
-}
-
-template <class Epi>
-static void launch_inv_impl(PlanTable& pt, const ConvPlan& p, const float2* spec, Epi e, cudaStream_t s) {
-  if (p.items_inv.empty()) return;
-  auto k = plane_inv_kernel<Epi>;
-  set_smem(k, p.smem_plane);
-  k<<<(int)p.items_inv.size(), kThreads, p.smem_plane, s>>>(p.d_tiles.as<TileDesc>(),
-                                                             p.d_items_inv.as<int2>(), pt.device(), spec, e);
-  MVD_CHECK(cudaGetLastError());
-  count_launch();
-}
-
-void launch_fwd_mirror(PlanTable& pt, const ConvPlan& p, const float* vol, float2* spec, cudaStream_t s) {
-  GatherMirror g{{vol, p.nx, p.ny, p.nz}};
-  launch_fwd_impl(pt, p, p.d_tiles.as<TileDesc>(), p.d_items_fwd.as<int2>(), (int)p.items_fwd.size(),
-                  p.smem_plane, spec, g, s);
-}
-
-void launch_fwd_value(PlanTable& pt, const ConvPlan& p, const float* vol, float value, float2* spec,
-                      cudaStream_t s) {
-  GatherValue g{{vol, p.nx, p.ny, p.nz}, value};
-  launch_fwd_impl(pt, p, p.d_tiles.as<TileDesc>(), p.d_items_fwd.as<int2>(), (int)p.items_fwd.size(),
-                  p.smem_plane, spec, g, s);
-}
-
-void launch_z(PlanTable& pt, const ConvPlan& p, float2* spec, const float2* otf, cudaStream_t s) {
-  if (p.items_z.empty()) return;
-  auto k = zpass_kernel<0>;
-  set_smem(k, p.smem_z);
-  k<<<(int)p.items_z.size(), kThreads, p.smem_z, s>>>(p.d_tiles.as<TileDesc>(), p.d_items_z.as<int2>(),
-                                                       pt.device(), spec, otf, 1.f);
-  MVD_CHECK(cudaGetLastError());
-  count_launch();
-}
-
-void launch_inv_store(PlanTable& pt, const ConvPlan& p, const float2* spec, float* out, cudaStream_t s) {
-  EpiStore e{out, p.nx, p.ny};
-  launch_inv_impl(pt, p, spec, e, s);
-}
-
-void launch_inv_quotient(PlanTable& pt, const ConvPlan& p, const float2* spec, const float* img,
-                         float* q, cudaStream_t s) {
-  EpiQuotient e{img, q, p.nx, p.ny};
-  launch_inv_impl(pt, p, spec, e, s);
-}
-
-void launch_inv_update(PlanTable& pt, const ConvPlan& p, const float2* spec, float* psi,
-                       const float* weight, float lambda, double* stat_sum, unsigned* stat_max,
-                       cudaStream_t s) {
-  EpiUpdate e{psi, weight, lambda, stat_sum, stat_max, p.nx, p.ny, 0.f, 0.f};
-  launch_inv_impl(pt, p, spec, e, s);
 }
 
 void convolve(PlanTable& pt, const ConvPlan& plan, const float* in, Ext ext, float value,
@@ -395,14 +343,10 @@ void build_otf(PlanTable& pt, const ConvPlan& plan, const float* kernel, float2*
   MVD_CHECK(cudaMemcpyAsync(dt.p, &t, sizeof(TileDesc), cudaMemcpyHostToDevice, s));
   MVD_CHECK(cudaMemcpyAsync(df.p, fwd.data(), fwd.size() * sizeof(int2), cudaMemcpyHostToDevice, s));
   MVD_CHECK(cudaMemcpyAsync(dz.p, zz.data(), zz.size() * sizeof(int2), cudaMemcpyHostToDevice, s));
-  GatherValue g{{scratch.as<float>(), tx, ty, tz}, 0.f};
-  launch_fwd_impl(pt, plan, dt.as<TileDesc>(), df.as<int2>(), (int)fwd.size(), plan.smem_plane, otf, g, s);
-  auto k = zpass_kernel<1>;
-  set_smem(k, plan.smem_z);
-  k<<<(int)zz.size(), kThreads, plan.smem_z, s>>>(dt.as<TileDesc>(), dz.as<int2>(), pt.device(), otf,
-                                                 nullptr, (float)(1.0 / ((double)tx * ty * tz)));
-  MVD_CHECK(cudaGetLastError());
-  count_launch();
+  launch_fwd_value_items(pt, plan, dt.as<TileDesc>(), df.as<int2>(), (int)fwd.size(), scratch.as<float>(), tx, ty, tz,
+                         0.f, otf, s);
+  launch_z_forward_scaled(pt, plan, dt.as<TileDesc>(), dz.as<int2>(), (int)zz.size(), otf,
+                          (float)(1.0 / ((double)tx * ty * tz)), s);
   // the temporary tables are freed when this returns: wait for the launches that read them
   MVD_CHECK(cudaStreamSynchronize(s));
 }

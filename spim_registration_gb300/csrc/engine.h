@@ -101,6 +101,20 @@ enum class Ext { Mirror = 0, Value = 1 };
 void convolve(PlanTable& pt, const ConvPlan& plan, const float* in, Ext ext, float value,
               const float2* otf, float2* spec, float* out, cudaStream_t s);
 
+// Raise a kernel's dynamic shared-memory limit (cached per device, kernel and size).
+void set_smem_raw(const void* kernel, size_t bytes);
+template <class K>
+inline void set_smem(K kernel, size_t bytes) {
+  set_smem_raw(reinterpret_cast<const void*>(kernel), bytes);
+}
+
+// Forward plane pass over explicit tile / item tables, gathering from a (vx, vy, vz) volume
+// with a constant border value; and the forward-only, scaled z pass (OTF preparation).
+void launch_fwd_value_items(PlanTable& pt, const ConvPlan& p, const TileDesc* tiles, const int2* items, int nitems,
+                            const float* vol, int vx, int vy, int vz, float value, float2* spec, cudaStream_t s);
+void launch_z_forward_scaled(PlanTable& pt, const ConvPlan& p, const TileDesc* tiles, const int2* items, int nitems,
+                             float2* spec, float scale, cudaStream_t s);
+
 // The three passes, for fused use by the deconvolution handle.
 void launch_fwd_mirror(PlanTable& pt, const ConvPlan& p, const float* vol, float2* spec, cudaStream_t s);
 void launch_fwd_value(PlanTable& pt, const ConvPlan& p, const float* vol, float value, float2* spec,

@@ -1,28 +1,37 @@
-// Block-cooperative mixed-radix Stockham FFT in shared memory (FP32), sm_103a.
+// Large-radix Stockham FFT building blocks for sm_103a (FP32).
 //
-// One CTA transforms `count` independent complex sequences of length N that live in shared
-// memory at  d[batch * bs + n * es].  Each stage of radix R reads a butterfly's R inputs into
-// registers, twiddles, runs the R-point DFT in registers and writes the R outputs to the
-// other of two buffers in Stockham (self-sorting) order, so no bit-reversal pass is needed
-// and a thread never holds more than one butterfly.  Butterflies are assigned batch-fastest,
-// which makes both row transforms (es = 1, odd bs) and column transforms (bs = 1) free of
-// shared-memory bank conflicts.
+// A transform of length N = R_0 R_1 ... R_{S-1} (each R_s <= 16, S usually 2) runs as S
+// stages.  In stage s every butterfly reads R_s values (stride N / R_s), twiddles them, runs
+// an R_s-point DFT in registers and writes them in Stockham (self-sorting) order.  Loads and
+// stores go through functors, so the first stage can read straight from global memory, the
+// last stage can write straight to global memory (or into an epilogue), and only the S - 1
+// exchanges in between touch shared memory.  For a convolution the forward transform's last
+// stage, the pointwise product with the kernel spectrum and the inverse transform's first
+// stage (radix order reversed) run in the same registers, with no exchange at all.
 //
-// Radices: 2, 3, 4, 5, 7, 8.  Twiddles come from a per-length table exp(-2 pi i k / N) that
-// the host computes in double precision.
+// Butterfly b of `count` sequences maps to (batch, j) either batch-fastest (consecutive
+// threads take consecutive sequences: column transforms and pencils, coalesced and free of
+// bank conflicts) or j-fastest (consecutive threads take consecutive positions of one
+// sequence: row transforms that load from or store to global memory).
+//
+// Twiddles between stages come from a per-length table exp(-2 pi i k / N) computed in double
+// on the host; the internal roots of the composite register DFTs are compile-time tables
+// (dft_consts.cuh).
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "dft_consts.cuh"
+
 namespace mvd {
 
-constexpr int kMaxStages = 12;
+constexpr int kMaxStages = 6;
 
 // Runtime plan of one transform length (device copy lives in a plan table).
 struct FftPlan {
   int n;                    // transform length
   int nstages;              // number of radix stages
-  int radix[kMaxStages];    // radices, product == n
+  int radix[kMaxStages];    // radices (each in {2,3,4,5,6,7,8,9,10,12,14,15,16}), product == n
   const float2* tw;         // exp(-2 pi i k / n), k in [0, n)
   const float2* tw_r2c;     // for the real-input length 2n: exp(-2 pi i k / (2n)), k in [0, n]
 };
@@ -45,6 +54,11 @@ __device__ __forceinline__ float2 mul_mi(float2 a) {
 // ---------------------------------------------------------------------------------------
 template <int R, bool INV>
 struct Dft;
+
+template <bool INV>
+struct Dft<1, INV> {
+  __device__ __forceinline__ static void run(float2*) {}
+};
 
 template <bool INV>
 struct Dft<2, INV> {
@@ -71,12 +85,10 @@ template <bool INV>
 struct Dft<8, INV> {
   __device__ __forceinline__ static void run(float2* v) {
     const float h = 0.70710678118654752440f;  // sqrt(1/2)
-    // radix-2 split: even / odd samples, then two 4-point DFTs
     float2 e[4] = {v[0], v[2], v[4], v[6]};
     float2 o[4] = {v[1], v[3], v[5], v[7]};
     Dft<4, INV>::run(e);
     Dft<4, INV>::run(o);
-    // twiddles w8^k for k = 1..3 (forward: exp(-i pi k / 4))
     float2 o1 = o[1], o2 = o[2], o3 = o[3];
     o[1] = INV ? make_float2(h * (o1.x - o1.y), h * (o1.x + o1.y))
                : make_float2(h * (o1.x + o1.y), h * (o1.y - o1.x));
@@ -151,7 +163,7 @@ struct Dft<7, INV> {
       for (int n = 1; n <= 3; ++n) {
         const int idx = (k * n) % 7;  // cos(2 pi k n / 7) = c[min(idx, 7-idx) - 1]
         const int j = (idx <= 3 ? idx : 7 - idx) - 1;
-        const float sg = idx <= 3 ? 1.f : -1.f;  // sin(2 pi k n / 7) sign
+        const float sg = idx <= 3 ? 1.f : -1.f;  // sign of sin(2 pi k n / 7)
         a.x += c[j] * p[n - 1].x;
         a.y += c[j] * p[n - 1].y;
         b.x += sg * s[j] * m[n - 1].x;
@@ -166,25 +178,77 @@ struct Dft<7, INV> {
   }
 };
 
+// R = A * B by one Cooley-Tukey split: n = B n1 + n2, k = k1 + A k2;
+// X[k1 + A k2] = sum_n2 W_B^{n2 k2} W_R^{n2 k1} sum_n1 x[B n1 + n2] W_A^{n1 k1}
+template <int A, int B, bool INV>
+struct DftAB {
+  __device__ __forceinline__ static void run(float2* v) {
+    constexpr int R = A * B;
+    float2 y[B][A];
+#pragma unroll
+    for (int n2 = 0; n2 < B; ++n2) {
+      float2 t[A];
+#pragma unroll
+      for (int n1 = 0; n1 < A; ++n1) t[n1] = v[B * n1 + n2];
+      Dft<A, INV>::run(t);
+#pragma unroll
+      for (int k1 = 0; k1 < A; ++k1) {
+        if ((n2 * k1) % R == 0) {
+          y[n2][k1] = t[k1];
+        } else {
+          float2 w = wconst<R>((n2 * k1) % R);
+          if (INV) w.y = -w.y;
+          y[n2][k1] = cmul(t[k1], w);
+        }
+      }
+    }
+#pragma unroll
+    for (int k1 = 0; k1 < A; ++k1) {
+      float2 t[B];
+#pragma unroll
+      for (int n2 = 0; n2 < B; ++n2) t[n2] = y[n2][k1];
+      Dft<B, INV>::run(t);
+#pragma unroll
+      for (int k2 = 0; k2 < B; ++k2) v[k1 + A * k2] = t[k2];
+    }
+  }
+};
+
+template <bool INV> struct Dft<6, INV> : DftAB<2, 3, INV> {};
+template <bool INV> struct Dft<9, INV> : DftAB<3, 3, INV> {};
+template <bool INV> struct Dft<10, INV> : DftAB<2, 5, INV> {};
+template <bool INV> struct Dft<12, INV> : DftAB<4, 3, INV> {};
+template <bool INV> struct Dft<14, INV> : DftAB<2, 7, INV> {};
+template <bool INV> struct Dft<15, INV> : DftAB<3, 5, INV> {};
+template <bool INV> struct Dft<16, INV> : DftAB<4, 4, INV> {};
+
 // ---------------------------------------------------------------------------------------
-// One Stockham stage of radix R, out of place (src -> dst), no barrier inside.
-// Butterfly b of `count` sequences: batch = b % count (fastest), j = b / count.
+// butterfly index mapping
 // ---------------------------------------------------------------------------------------
-template <int R, bool INV>
-__device__ __forceinline__ void stockham_stage(const float2* __restrict__ src, float2* __restrict__ dst, int N,
-                                               int Ns, int count, int es, int bs,
-                                               const float2* __restrict__ tw) {
+template <bool JFAST>
+__device__ __forceinline__ void butterfly_index(int b, int count, int NR, int& batch, int& j) {
+  if (JFAST) {
+    batch = b / NR;
+    j = b - batch * NR;
+  } else {
+    j = b / count;
+    batch = b - j * count;
+  }
+}
+
+// One radix-R Stockham stage of `count` sequences: ld(batch, i) -> float2, st(batch, i, v).
+template <int R, bool INV, bool JFAST, class LD, class ST>
+__device__ __forceinline__ void stage_r(int N, int Ns, int count, const float2* __restrict__ tw, const LD& ld,
+                                        const ST& st) {
   const int NR = N / R;
   const int nb = count * NR;
   const int twstride = N / (Ns * R);
-#pragma unroll 2
   for (int b = threadIdx.x; b < nb; b += blockDim.x) {
-    const int j = b / count;
-    const int batch = b - j * count;
-    const float2* s = src + batch * bs + j * es;
+    int batch, j;
+    butterfly_index<JFAST>(b, count, NR, batch, j);
     float2 v[R];
 #pragma unroll
-    for (int r = 0; r < R; ++r) v[r] = s[r * NR * es];
+    for (int r = 0; r < R; ++r) v[r] = ld(batch, j + r * NR);
     const int k = j % Ns;
     if (k != 0) {
 #pragma unroll
@@ -195,38 +259,90 @@ __device__ __forceinline__ void stockham_stage(const float2* __restrict__ src, f
       }
     }
     Dft<R, INV>::run(v);
-    float2* d = dst + batch * bs + ((j - k) * R + k) * es;
+    const int base = (j - k) * R + k;
 #pragma unroll
-    for (int r = 0; r < R; ++r) d[r * Ns * es] = v[r];
+    for (int r = 0; r < R; ++r) st(batch, base + r * Ns, v[r]);
   }
 }
 
-// Full transform of `count` sequences with the plan `p` (read from global memory), ping-pong
-// between the buffers `cur` and `oth`; on return `cur` holds the result.
-template <bool INV>
-__device__ __forceinline__ void block_fft(float2*& cur, float2*& oth, const FftPlan* __restrict__ p, int count,
-                                          int es, int bs) {
-  const int n = __ldg(&p->n);
-  const int ns = __ldg(&p->nstages);
-  const float2* tw = p->tw;
-  int Ns = 1;
-  for (int s = 0; s < ns; ++s) {
-    const int R = __ldg(&p->radix[s]);
-    switch (R) {
-      case 2: stockham_stage<2, INV>(cur, oth, n, Ns, count, es, bs, tw); break;
-      case 3: stockham_stage<3, INV>(cur, oth, n, Ns, count, es, bs, tw); break;
-      case 4: stockham_stage<4, INV>(cur, oth, n, Ns, count, es, bs, tw); break;
-      case 5: stockham_stage<5, INV>(cur, oth, n, Ns, count, es, bs, tw); break;
-      case 7: stockham_stage<7, INV>(cur, oth, n, Ns, count, es, bs, tw); break;
-      default: stockham_stage<8, INV>(cur, oth, n, Ns, count, es, bs, tw); break;
-    }
-    __syncthreads();
-    float2* t = cur;
-    cur = oth;
-    oth = t;
-    Ns *= R;
+template <bool INV, bool JFAST, class LD, class ST>
+__device__ __forceinline__ void stage(int R, int N, int Ns, int count, const float2* __restrict__ tw, const LD& ld,
+                                      const ST& st) {
+  switch (R) {
+    case 2: stage_r<2, INV, JFAST>(N, Ns, count, tw, ld, st); break;
+    case 3: stage_r<3, INV, JFAST>(N, Ns, count, tw, ld, st); break;
+    case 4: stage_r<4, INV, JFAST>(N, Ns, count, tw, ld, st); break;
+    case 5: stage_r<5, INV, JFAST>(N, Ns, count, tw, ld, st); break;
+    case 6: stage_r<6, INV, JFAST>(N, Ns, count, tw, ld, st); break;
+    case 7: stage_r<7, INV, JFAST>(N, Ns, count, tw, ld, st); break;
+    case 8: stage_r<8, INV, JFAST>(N, Ns, count, tw, ld, st); break;
+    case 9: stage_r<9, INV, JFAST>(N, Ns, count, tw, ld, st); break;
+    case 10: stage_r<10, INV, JFAST>(N, Ns, count, tw, ld, st); break;
+    case 12: stage_r<12, INV, JFAST>(N, Ns, count, tw, ld, st); break;
+    case 14: stage_r<14, INV, JFAST>(N, Ns, count, tw, ld, st); break;
+    case 15: stage_r<15, INV, JFAST>(N, Ns, count, tw, ld, st); break;
+    case 16: stage_r<16, INV, JFAST>(N, Ns, count, tw, ld, st); break;
+    default: stage_r<1, INV, JFAST>(N, Ns, count, tw, ld, st); break;  // length-1 transform: copy
   }
 }
+
+// Forward last stage (radix R, Ns = N/R) + pointwise product + inverse first stage (radix R,
+// Ns = 1) in the same registers.  mul(batch, k, v) returns v times the spectrum at natural
+// index k.  Output: the inverse first stage's Stockham order (index j R + r).
+template <int R, class LD, class MUL, class ST>
+__device__ __forceinline__ void zmid_r(int N, int count, const float2* __restrict__ tw, const LD& ld, const MUL& mul,
+                                       const ST& st) {
+  const int NR = N / R;
+  const int nb = count * NR;
+  for (int b = threadIdx.x; b < nb; b += blockDim.x) {
+    int batch, j;
+    butterfly_index<false>(b, count, NR, batch, j);
+    float2 v[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) v[r] = ld(batch, j + r * NR);
+    if (j != 0) {
+#pragma unroll
+      for (int r = 1; r < R; ++r) v[r] = cmul(v[r], __ldg(tw + r * j));
+    }
+    Dft<R, false>::run(v);
+#pragma unroll
+    for (int r = 0; r < R; ++r) v[r] = mul(batch, j + r * NR, v[r]);
+    Dft<R, true>::run(v);
+#pragma unroll
+    for (int r = 0; r < R; ++r) st(batch, j * R + r, v[r]);
+  }
+}
+
+template <class LD, class MUL, class ST>
+__device__ __forceinline__ void zmid(int R, int N, int count, const float2* __restrict__ tw, const LD& ld,
+                                     const MUL& mul, const ST& st) {
+  switch (R) {
+    case 2: zmid_r<2>(N, count, tw, ld, mul, st); break;
+    case 3: zmid_r<3>(N, count, tw, ld, mul, st); break;
+    case 4: zmid_r<4>(N, count, tw, ld, mul, st); break;
+    case 5: zmid_r<5>(N, count, tw, ld, mul, st); break;
+    case 6: zmid_r<6>(N, count, tw, ld, mul, st); break;
+    case 7: zmid_r<7>(N, count, tw, ld, mul, st); break;
+    case 8: zmid_r<8>(N, count, tw, ld, mul, st); break;
+    case 9: zmid_r<9>(N, count, tw, ld, mul, st); break;
+    case 10: zmid_r<10>(N, count, tw, ld, mul, st); break;
+    case 12: zmid_r<12>(N, count, tw, ld, mul, st); break;
+    case 14: zmid_r<14>(N, count, tw, ld, mul, st); break;
+    case 15: zmid_r<15>(N, count, tw, ld, mul, st); break;
+    case 16: zmid_r<16>(N, count, tw, ld, mul, st); break;
+    default: zmid_r<1>(N, count, tw, ld, mul, st); break;
+  }
+}
+
+// ---------------------------------------------------------------------------------------
+// Shared-memory accessor: element (batch, i) at p[batch * bs + i * es]
+// ---------------------------------------------------------------------------------------
+struct SmemRef {
+  float2* p;
+  int es, bs;
+  __device__ __forceinline__ float2 operator()(int batch, int i) const { return p[batch * bs + i * es]; }
+  __device__ __forceinline__ void operator()(int batch, int i, float2 v) const { p[batch * bs + i * es] = v; }
+};
 
 // ---------------------------------------------------------------------------------------
 // Real <-> half-complex post/pre-processing of rows.  A row of 2M reals packed as M complex
@@ -234,9 +350,9 @@ __device__ __forceinline__ void block_fft(float2*& cur, float2*& oth, const FftP
 // into X[k], k = 0..M, of the length-2M real transform, writing X[M] to slot M.
 // The pre-step is its inverse up to a factor 2 (together with an unnormalised inverse
 // FFT_M it yields 2M * x).  `tw2` = exp(-2 pi i k / (2M)), k in [0, M].
+// Rows are d + r * pitch for r in [0, rows); no barrier inside.
 // ---------------------------------------------------------------------------------------
-__device__ __forceinline__ void r2c_post(float2* d, int rows, int M, int pitch,
-                                         const float2* __restrict__ tw2) {
+__device__ __forceinline__ void r2c_post(float2* d, int rows, int M, int pitch, const float2* __restrict__ tw2) {
   const int half = M / 2;  // pairs (k, M-k) for k = 0..half
   const int total = rows * (half + 1);
   for (int i = threadIdx.x; i < total; i += blockDim.x) {
@@ -251,26 +367,23 @@ __device__ __forceinline__ void r2c_post(float2* d, int rows, int M, int pitch,
     }
     const int k2 = M - k;
     float2 zk = r[k], zc = r[k2];
-    // X[k] = (Zk + conj(Zc))/2 - i/2 * w^k (Zk - conj(Zc))
+    // X[k] = e - i w^k o,  e = (Zk + conj Zc)/2,  o = (Zk - conj Zc)/2
     float2 e = make_float2(0.5f * (zk.x + zc.x), 0.5f * (zk.y - zc.y));
-    float2 o = make_float2(0.5f * (zk.x - zc.x), 0.5f * (zk.y + zc.y));  // (Zk - conj Zc)/2
+    float2 o = make_float2(0.5f * (zk.x - zc.x), 0.5f * (zk.y + zc.y));
     float2 w = __ldg(tw2 + k);
     float2 wo = cmul(w, o);
-    float2 xk = make_float2(e.x + wo.y, e.y - wo.x);  // e - i * wo
+    float2 xk = make_float2(e.x + wo.y, e.y - wo.x);
     if (k2 == k) {
       r[k] = xk;
     } else {
       // X[M-k] = conj(e) - i conj(w^k o)   (uses w^{M-k} = -conj(w^k))
-      float2 xk2 = make_float2(e.x - wo.y, -e.y - wo.x);
       r[k] = xk;
-      r[k2] = xk2;
+      r[k2] = make_float2(e.x - wo.y, -e.y - wo.x);
     }
   }
-  __syncthreads();
 }
 
-__device__ __forceinline__ void c2r_pre(float2* d, int rows, int M, int pitch,
-                                        const float2* __restrict__ tw2) {
+__device__ __forceinline__ void c2r_pre(float2* d, int rows, int M, int pitch, const float2* __restrict__ tw2) {
   const int half = M / 2;
   const int total = rows * (half + 1);
   for (int i = threadIdx.x; i < total; i += blockDim.x) {
@@ -298,12 +411,10 @@ __device__ __forceinline__ void c2r_pre(float2* d, int rows, int M, int pitch,
     } else {
       // Z[M-k] = conj(e) + i w^k conj(o)   (uses conj(w^{M-k}) = -w^k)
       float2 wo2 = cmul(w, cconj(o));
-      float2 zk2 = make_float2(e.x - wo2.y, -e.y + wo2.x);
       r[k] = zk;
-      r[k2] = zk2;
+      r[k2] = make_float2(e.x - wo2.y, -e.y + wo2.x);
     }
   }
-  __syncthreads();
 }
 
 }  // namespace mvd

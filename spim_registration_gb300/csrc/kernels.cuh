@@ -21,10 +21,20 @@
 
 namespace mvd {
 
-constexpr int kThreads = 512;    // threads per CTA of the FFT kernels
+constexpr int kThreads = 512;    // threads per CTA of the plane kernels
+constexpr int kZThreads = 256;   // threads per CTA of the z-pencil kernel
 constexpr int kPlaneCap = 14336; // complex values of one shared-memory buffer (two are used)
-constexpr int kZChunk = 32;      // pencils per z-pass CTA
+constexpr int kZChunk = 16;      // pencils per z-pass CTA (16 complex = one 128-byte line)
 constexpr int kZPitch = kZChunk + 1;
+
+// Row pitch (complex values, odd) that holds a half-spectrum row of px = M + 1 values and
+// the skewed layout i + i/16 of a length-M row between the first two row stages.
+__host__ __device__ inline int row_pitch(int M) {
+  int p = M + 1;
+  const int skew = M + (M - 1) / 16 + 1;
+  if (skew > p) p = skew;
+  return (p & 1) ? p : p + 1;
+}
 
 struct TileDesc {
   int tx, ty, tz;        // FFT size of the tile
@@ -174,6 +184,159 @@ struct EpiUpdate {
 };
 
 // ------------------------------------------------------------------------------------------
+// load / store functors of the first and last FFT stages
+// ------------------------------------------------------------------------------------------
+// row element i of a row stored with the skew i + i/16 (used between row stages 0 and 1)
+struct SmemRowSkew {
+  float2* p;
+  int pitch;
+  __device__ __forceinline__ float2 operator()(int batch, int i) const { return p[batch * pitch + i + (i >> 4)]; }
+  __device__ __forceinline__ void operator()(int batch, int i, float2 v) const { p[batch * pitch + i + (i >> 4)] = v; }
+};
+
+template <class Gather>
+struct RowGather {  // packed pair (x[2n], x[2n+1]) of tile row `batch`, gathered from the volume
+  Gather g;
+  int ox, oy, gz;
+  __device__ __forceinline__ float2 operator()(int batch, int n) const {
+    const int gx = ox + 2 * n, gy = oy + batch;
+    return make_float2(g(gx, gy, gz), g(gx + 1, gy, gz));
+  }
+};
+
+struct SpecSliceLoad {  // spectrum slice [y][kx]: batch = kx, i = y
+  const float2* p;
+  int px;
+  __device__ __forceinline__ float2 operator()(int batch, int i) const { return __ldg(p + i * px + batch); }
+};
+
+struct SpecSliceStore {
+  float2* p;
+  int px;
+  __device__ __forceinline__ void operator()(int batch, int i, float2 v) const { p[i * px + batch] = v; }
+};
+
+struct PencilRef {  // pencil element: batch = pencil in the chunk, i = z
+  float2* p;
+  long long plane;
+  __device__ __forceinline__ float2 operator()(int batch, int i) const { return p[i * plane + batch]; }
+  __device__ __forceinline__ void operator()(int batch, int i, float2 v) const { p[i * plane + batch] = v; }
+};
+
+struct PencilScaledStore {
+  float2* p;
+  long long plane;
+  float scale;
+  __device__ __forceinline__ void operator()(int batch, int i, float2 v) const { p[i * plane + batch] = cscale(v, scale); }
+};
+
+struct OtfMul {
+  const float2* p;
+  long long plane;
+  __device__ __forceinline__ float2 operator()(int batch, int k, float2 v) const {
+    return cmul(v, __ldg(p + k * plane + batch));
+  }
+};
+
+template <class Epi>
+struct RowEpilogue {  // last inverse x stage: complex n of effective row `batch` = reals 2n, 2n+1
+  Epi* epi;
+  long long row0;     // global index of tile-local (x = 0, y = hy, z) in the volume
+  long long ystride;  // global stride of one row
+  int hx, ex;
+  __device__ __forceinline__ void operator()(int batch, int n, float2 v) const {
+    const long long g = row0 + batch * ystride;
+    const int x0 = 2 * n - hx;
+    if (x0 >= 0 && x0 < ex) (*epi)(g + x0, v.x);
+    if (x0 + 1 >= 0 && x0 + 1 < ex) (*epi)(g + x0 + 1, v.y);
+  }
+};
+
+// Stage dispatch over the shared-memory layouts: `skew_in` / `skew_out` select the skewed
+// row layout (i + i/16) for the buffer read / written.
+template <bool INV, bool JFAST, class LD>
+__device__ __forceinline__ void stage_to_smem(int R, int n, int Ns, int count, const float2* tw, const LD& ld,
+                                              float2* dst, int es, int bs, bool skew_out) {
+  if (skew_out)
+    stage<INV, JFAST>(R, n, Ns, count, tw, ld, SmemRowSkew{dst, bs});
+  else
+    stage<INV, JFAST>(R, n, Ns, count, tw, ld, SmemRef{dst, es, bs});
+}
+
+template <bool INV, bool JFAST, class ST>
+__device__ __forceinline__ void stage_from_smem(int R, int n, int Ns, int count, const float2* tw, float2* src,
+                                                int es, int bs, bool skew_in, const ST& st) {
+  if (skew_in)
+    stage<INV, JFAST>(R, n, Ns, count, tw, SmemRowSkew{src, bs}, st);
+  else
+    stage<INV, JFAST>(R, n, Ns, count, tw, SmemRef{src, es, bs}, st);
+}
+
+// All stages of one transform with the result left in shared memory: on return (after a
+// barrier) `cur` holds it in the plain layout.  Stage 0 loads with ld0 (global memory or
+// `cur`) and every stage writes the other buffer.  ROWS (row transforms, es == 1): j-fastest
+// butterflies and the skewed layout between stages 0 and 1.
+template <bool INV, bool ROWS, class LD0>
+__device__ __forceinline__ void run_transform_smem(const FftPlan* __restrict__ p, int count, const LD0& ld0,
+                                                   float2*& cur, float2*& oth, int es, int bs) {
+  const int n = __ldg(&p->n);
+  const int ns = __ldg(&p->nstages);
+  const float2* tw = p->tw;
+  int Ns = 1;
+  for (int s = 0; s < ns; ++s) {
+    const int R = __ldg(&p->radix[s]);
+    const bool skew_out = ROWS && s == 0 && ns > 1;
+    if (s == 0) {
+      stage_to_smem<INV, ROWS>(R, n, Ns, count, tw, ld0, oth, es, bs, skew_out);
+    } else {
+      if (ROWS && s == 1)
+        stage<INV, ROWS>(R, n, Ns, count, tw, SmemRowSkew{cur, bs}, SmemRef{oth, es, bs});
+      else
+        stage<INV, ROWS>(R, n, Ns, count, tw, SmemRef{cur, es, bs}, SmemRef{oth, es, bs});
+    }
+    __syncthreads();
+    float2* t = cur;
+    cur = oth;
+    oth = t;
+    Ns *= R;
+  }
+}
+
+// All stages of one transform with the last stage storing through `stl` (global memory or an
+// epilogue).  Stage 0 loads with ld0; the exchanges in between alternate the two buffers.
+template <bool INV, bool ROWS, class LD0, class STL>
+__device__ __forceinline__ void run_transform_to(const FftPlan* __restrict__ p, int count, const LD0& ld0,
+                                                 const STL& stl, float2*& cur, float2*& oth, int es, int bs) {
+  const int n = __ldg(&p->n);
+  const int ns = __ldg(&p->nstages);
+  const float2* tw = p->tw;
+  if (ns == 1) {
+    stage<INV, ROWS>(__ldg(&p->radix[0]), n, 1, count, tw, ld0, stl);
+    return;
+  }
+  int Ns = 1;
+  for (int s = 0; s < ns; ++s) {
+    const int R = __ldg(&p->radix[s]);
+    const bool skew_in = ROWS && s == 1;
+    if (s == ns - 1) {
+      stage_from_smem<INV, ROWS>(R, n, Ns, count, tw, cur, es, bs, skew_in, stl);
+    } else {
+      if (s == 0)
+        stage_to_smem<INV, ROWS>(R, n, Ns, count, tw, ld0, oth, es, bs, ROWS);
+      else if (skew_in)
+        stage<INV, ROWS>(R, n, Ns, count, tw, SmemRowSkew{cur, bs}, SmemRef{oth, es, bs});
+      else
+        stage<INV, ROWS>(R, n, Ns, count, tw, SmemRef{cur, es, bs}, SmemRef{oth, es, bs});
+      __syncthreads();
+      float2* t = cur;
+      cur = oth;
+      oth = t;
+    }
+    Ns *= R;
+  }
+}
+
+// ------------------------------------------------------------------------------------------
 // kernels (templated on gather / epilogue; instantiated in engine.cu)
 // ------------------------------------------------------------------------------------------
 template <class Gather>
@@ -185,27 +348,17 @@ plane_fwd_kernel(const TileDesc* __restrict__ tiles, const int2* __restrict__ it
   const TileDesc t = tiles[it.x];
   const int z = it.y;
   const int M = t.tx / 2;
-  const FftPlan* px_plan = plans + t.plan_x;
-  const FftPlan* py_plan = plans + t.plan_y;
   float2* cur = sm;
   float2* oth = sm + t.ty * t.pitch;
-  float* smf = reinterpret_cast<float*>(cur);
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
-  const int gz = t.oz + z;
-  for (int y = warp; y < t.ty; y += nwarps) {
-    const int gy = t.oy + y;
-    float* row = smf + 2 * y * t.pitch;
-    for (int x = lane; x < t.tx; x += 32) row[x] = gather(t.ox + x, gy, gz);
-  }
+  // x: R2C of every row (packed pairs gathered straight from the volume)
+  RowGather<Gather> ld0{gather, t.ox, t.oy, t.oz + z};
+  const FftPlan* pxp = plans + t.plan_x;
+  run_transform_smem<false, true>(pxp, t.ty, ld0, cur, oth, 1, t.pitch);
+  r2c_post(cur, t.ty, M, t.pitch, pxp->tw_r2c);
   __syncthreads();
-  block_fft<false>(cur, oth, px_plan, t.ty, 1, t.pitch);
-  r2c_post(cur, t.ty, M, t.pitch, px_plan->tw_r2c);
-  block_fft<false>(cur, oth, py_plan, t.px, t.pitch, 1);
-  float2* dst = spec + t.spec_off + (long long)z * t.ty * t.px;
-  for (int y = warp; y < t.ty; y += nwarps) {
-    const float2* row = cur + y * t.pitch;
-    for (int x = lane; x < t.px; x += 32) dst[y * t.px + x] = row[x];
-  }
+  // y: C2C of every column, last stage straight to the spectrum slice
+  SpecSliceStore st{spec + t.spec_off + (long long)z * t.ty * t.px, t.px};
+  run_transform_to<false, false>(plans + t.plan_y, t.px, SmemRef{cur, t.pitch, 1}, st, cur, oth, t.pitch, 1);
 }
 
 template <class Epi>
@@ -217,35 +370,27 @@ plane_inv_kernel(const TileDesc* __restrict__ tiles, const int2* __restrict__ it
   const TileDesc t = tiles[it.x];
   const int z = it.y;  // tile-local slice, inside the effective range
   const int M = t.tx / 2;
-  const FftPlan* px_plan = plans + t.plan_x;
-  const FftPlan* py_plan = plans + t.plan_y;
   float2* cur = sm;
   float2* oth = sm + t.ty * t.pitch;
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
-  const float2* src = spec + t.spec_off + (long long)z * t.ty * t.px;
-  for (int y = warp; y < t.ty; y += nwarps) {
-    float2* row = cur + y * t.pitch;
-    for (int x = lane; x < t.px; x += 32) row[x] = __ldg(src + y * t.px + x);
-  }
+  // y: inverse C2C of every column, first stage straight from the spectrum slice
+  SpecSliceLoad ld{spec + t.spec_off + (long long)z * t.ty * t.px, t.px};
+  run_transform_smem<true, false>(plans + t.plan_y, t.px, ld, cur, oth, t.pitch, 1);
+  // only the effective rows go on: C2R pre-step and the inverse x transform
+  float2* rows = cur + t.hy * t.pitch;
+  float2* rows_oth = oth + t.hy * t.pitch;
+  c2r_pre(rows, t.ey, M, t.pitch, plans[t.plan_x].tw_r2c);
   __syncthreads();
-  block_fft<true>(cur, oth, py_plan, t.px, t.pitch, 1);
-  c2r_pre(cur, t.ty, M, t.pitch, px_plan->tw_r2c);
-  block_fft<true>(cur, oth, px_plan, t.ty, 1, t.pitch);
-  const float* smf = reinterpret_cast<const float*>(cur);
   const long long gz = t.oz + z;
+  RowEpilogue<Epi> st{&epi, (gz * epi.ny + (t.oy + t.hy)) * (long long)epi.nx + t.ox + t.hx, (long long)epi.nx,
+                      t.hx, t.ex};
   epi.acc_init();
-  for (int y = warp; y < t.ey; y += nwarps) {
-    const int ly = t.hy + y;
-    const long long grow = (gz * epi.ny + (t.oy + ly)) * (long long)epi.nx + t.ox;
-    const float* row = smf + 2 * ly * t.pitch;
-    for (int x = lane; x < t.ex; x += 32) epi(grow + t.hx + x, row[t.hx + x]);
-  }
+  run_transform_to<true, true>(plans + t.plan_x, t.ey, SmemRef{rows, 1, t.pitch}, st, rows, rows_oth, 1, t.pitch);
   epi.finish();
 }
 
-// MODE 0: forward z, multiply by OTF, inverse z.  MODE 1: forward z and scale (OTF build).
+// MODE 0: forward z, multiply by the OTF, inverse z.  MODE 1: forward z and scale (OTF build).
 template <int MODE>
-__global__ void __launch_bounds__(kThreads, 1)
+__global__ void __launch_bounds__(kZThreads)
 zpass_kernel(const TileDesc* __restrict__ tiles, const int2* __restrict__ items,
              const FftPlan* __restrict__ plans, float2* __restrict__ spec,
              const float2* __restrict__ otf, float scale) {
@@ -258,29 +403,56 @@ zpass_kernel(const TileDesc* __restrict__ tiles, const int2* __restrict__ items,
   const FftPlan* pz = plans + t.plan_z;
   float2* cur = sm;
   float2* oth = sm + t.tz * kZPitch;
-  float2* base = spec + t.spec_off + p0;
-  for (int i = threadIdx.x; i < t.tz * kZChunk; i += blockDim.x) {
-    const int z = i / kZChunk, c = i % kZChunk;
-    if (c < count) cur[z * kZPitch + c] = base[z * plane + c];
+  PencilRef g{spec + t.spec_off + p0, plane};
+  const int n = __ldg(&pz->n);
+  const int ns = __ldg(&pz->nstages);
+  const float2* tw = pz->tw;
+  if (MODE == 1) {
+    run_transform_to<false, false>(pz, count, g, PencilScaledStore{g.p, plane, scale}, cur, oth, kZPitch, 1);
+    return;
   }
-  __syncthreads();
-  block_fft<false>(cur, oth, pz, count, kZPitch, 1);
-  if (MODE == 0) {
-    const float2* o = otf + t.otf_off + p0;
-    for (int i = threadIdx.x; i < t.tz * kZChunk; i += blockDim.x) {
-      const int z = i / kZChunk, c = i % kZChunk;
-      if (c < count) cur[z * kZPitch + c] = cmul(cur[z * kZPitch + c], __ldg(o + z * plane + c));
+  OtfMul mul{otf + t.otf_off + p0, plane};
+  if (ns == 1) {
+    zmid(__ldg(&pz->radix[0]), n, count, tw, g, mul, g);
+    return;
+  }
+  // forward stages 0 .. ns-2
+  int Ns = 1;
+  for (int s = 0; s < ns - 1; ++s) {
+    const int R = __ldg(&pz->radix[s]);
+    if (s == 0) {
+      stage<false, false>(R, n, Ns, count, tw, g, SmemRef{cur, kZPitch, 1});
+    } else {
+      stage<false, false>(R, n, Ns, count, tw, SmemRef{cur, kZPitch, 1}, SmemRef{oth, kZPitch, 1});
+      float2* tmp = cur;
+      cur = oth;
+      oth = tmp;
     }
     __syncthreads();
-    block_fft<true>(cur, oth, pz, count, kZPitch, 1);
+    Ns *= R;
   }
-  for (int i = threadIdx.x; i < t.tz * kZChunk; i += blockDim.x) {
-    const int z = i / kZChunk, c = i % kZChunk;
-    if (c < count) {
-      float2 v = cur[z * kZPitch + c];
-      if (MODE == 1) v = cscale(v, scale);
-      base[z * plane + c] = v;
+  // forward last stage, product with the OTF, inverse first stage
+  zmid(__ldg(&pz->radix[ns - 1]), n, count, tw, SmemRef{cur, kZPitch, 1}, mul, SmemRef{oth, kZPitch, 1});
+  __syncthreads();
+  {
+    float2* tmp = cur;
+    cur = oth;
+    oth = tmp;
+  }
+  // inverse stages 1 .. ns-1 use the radices in reverse order
+  Ns = __ldg(&pz->radix[ns - 1]);
+  for (int i = 1; i < ns; ++i) {
+    const int R = __ldg(&pz->radix[ns - 1 - i]);
+    if (i == ns - 1) {
+      stage<true, false>(R, n, Ns, count, tw, SmemRef{cur, kZPitch, 1}, g);
+    } else {
+      stage<true, false>(R, n, Ns, count, tw, SmemRef{cur, kZPitch, 1}, SmemRef{oth, kZPitch, 1});
+      __syncthreads();
+      float2* tmp = cur;
+      cur = oth;
+      oth = tmp;
     }
+    Ns *= R;
   }
 }
 

@@ -135,8 +135,7 @@ extern "C" int mvd_convolve3d_device_noalloc(const float* in, float* out, const 
     Axis bx{}, by{}, bz{};
     for (auto& a : ox)
       for (auto& b : oy) {
-        const int pxa = a.T / 2 + 1;
-        if ((long long)((pxa & 1) ? pxa : pxa + 1) * b.T > kPlaneCap) continue;
+        if ((long long)row_pitch(a.T / 2) * b.T > kPlaneCap) continue;
         for (auto& c : oz) {
           const double nt = (double)a.n * b.n * c.n;
           const double cost = nt * a.T * b.T * c.T * (1.0 + 1e-3 * nt);
@@ -153,7 +152,7 @@ extern "C" int mvd_convolve3d_device_noalloc(const float* in, float* out, const 
       return MVD_ERR_ARG;
     }
     const int px = bx.T / 2 + 1;
-    const int pitch = (px & 1) ? px : px + 1;
+    const int pitch = row_pitch(bx.T / 2);
     const int lens[3] = {bx.T / 2, by.T, bz.T};
 
     // FFT plans for the three lengths, twiddles computed in double on the host
@@ -163,7 +162,7 @@ extern "C" int mvd_convolve3d_device_noalloc(const float* in, float* out, const 
       const int n = lens[i];
       FftPlan p{};
       p.n = n;
-      std::vector<int> rad = n == 1 ? std::vector<int>{} : factorize(n);
+      std::vector<int> rad = factorize(n);
       p.nstages = (int)rad.size();
       for (size_t r = 0; r < rad.size(); ++r) p.radix[r] = rad[r];
       plans[i] = p;
@@ -274,7 +273,7 @@ extern "C" int mvd_convolve3d_device_noalloc(const float* in, float* out, const 
         GatherValue{{d_place, bx.T, by.T, bz.T}, 0.f});
     MVD_CHECK(cudaGetLastError());
     smem_attr(zpass_kernel<1>, smem_z);
-    zpass_kernel<1><<<(int)otf_z.size(), kThreads, smem_z, s>>>(d_tiles, reinterpret_cast<const int2*>(base + o_oz),
+    zpass_kernel<1><<<(int)otf_z.size(), kZThreads, smem_z, s>>>(d_tiles, reinterpret_cast<const int2*>(base + o_oz),
                                                                  d_plans, d_otf, nullptr,
                                                                  (float)(1.0 / ((double)bx.T * by.T * bz.T)));
     MVD_CHECK(cudaGetLastError());
@@ -291,7 +290,7 @@ extern "C" int mvd_convolve3d_device_noalloc(const float* in, float* out, const 
     }
     MVD_CHECK(cudaGetLastError());
     smem_attr(zpass_kernel<0>, smem_z);
-    zpass_kernel<0><<<(int)zz.size(), kThreads, smem_z, s>>>(d_tiles, reinterpret_cast<const int2*>(base + o_z),
+    zpass_kernel<0><<<(int)zz.size(), kZThreads, smem_z, s>>>(d_tiles, reinterpret_cast<const int2*>(base + o_z),
                                                               d_plans, d_spec, d_otf, 1.f);
     MVD_CHECK(cudaGetLastError());
     if (!inv.empty()) {

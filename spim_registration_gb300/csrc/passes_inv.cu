@@ -1,0 +1,34 @@
+// Instantiations and launches of the inverse plane pass (split from engine.cu so the library builds in parallel).
+#include "engine.h"
+
+namespace mvd {
+
+template <class Epi>
+static void launch_inv_impl(PlanTable& pt, const ConvPlan& p, const float2* spec, Epi e, cudaStream_t s) {
+  if (p.items_inv.empty()) return;
+  auto k = plane_inv_kernel<Epi>;
+  set_smem(k, p.smem_plane);
+  k<<<(int)p.items_inv.size(), kThreads, p.smem_plane, s>>>(p.d_tiles.as<TileDesc>(), p.d_items_inv.as<int2>(),
+                                                             pt.device(), spec, e);
+  MVD_CHECK(cudaGetLastError());
+  count_launch();
+}
+
+void launch_inv_store(PlanTable& pt, const ConvPlan& p, const float2* spec, float* out, cudaStream_t s) {
+  EpiStore e{out, p.nx, p.ny};
+  launch_inv_impl(pt, p, spec, e, s);
+}
+
+void launch_inv_quotient(PlanTable& pt, const ConvPlan& p, const float2* spec, const float* img, float* q,
+                         cudaStream_t s) {
+  EpiQuotient e{img, q, p.nx, p.ny};
+  launch_inv_impl(pt, p, spec, e, s);
+}
+
+void launch_inv_update(PlanTable& pt, const ConvPlan& p, const float2* spec, float* psi, const float* weight,
+                       float lambda, double* stat_sum, unsigned* stat_max, cudaStream_t s) {
+  EpiUpdate e{psi, weight, lambda, stat_sum, stat_max, p.nx, p.ny, 0.f, 0.f};
+  launch_inv_impl(pt, p, spec, e, s);
+}
+
+}  // namespace mvd

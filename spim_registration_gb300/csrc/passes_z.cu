@@ -1,0 +1,26 @@
+// Instantiations and launches of the z-pencil pass (split from engine.cu so the library builds in parallel).
+#include "engine.h"
+
+namespace mvd {
+
+void launch_z(PlanTable& pt, const ConvPlan& p, float2* spec, const float2* otf, cudaStream_t s) {
+  if (p.items_z.empty()) return;
+  auto k = zpass_kernel<0>;
+  set_smem(k, p.smem_z);
+  k<<<(int)p.items_z.size(), kZThreads, p.smem_z, s>>>(p.d_tiles.as<TileDesc>(), p.d_items_z.as<int2>(), pt.device(),
+                                                        spec, otf, 1.f);
+  MVD_CHECK(cudaGetLastError());
+  count_launch();
+}
+
+void launch_z_forward_scaled(PlanTable& pt, const ConvPlan& p, const TileDesc* tiles, const int2* items, int nitems,
+                             float2* spec, float scale, cudaStream_t s) {
+  if (nitems == 0) return;
+  auto k = zpass_kernel<1>;
+  set_smem(k, p.smem_z);
+  k<<<nitems, kZThreads, p.smem_z, s>>>(tiles, items, pt.device(), spec, nullptr, scale);
+  MVD_CHECK(cudaGetLastError());
+  count_launch();
+}
+
+}  // namespace mvd
