@@ -117,10 +117,26 @@ class ClockSampler:
 
 
 def make_problem(workload):
+    """The workload's seeded inputs; MVD_PROBLEM_CACHE=<dir> keeps them between runs."""
     from spim_registration_gb300 import synthetic as S
 
     cfg, shape, psf, _ = WORKLOADS[workload]
-    return S.make_problem(cfg, shape_xyz=shape, psf_size_xyz=psf)
+    cache = os.environ.get("MVD_PROBLEM_CACHE")
+    path = os.path.join(cache, workload + ".npz") if cache else None
+    if path and os.path.exists(path):
+        z = np.load(path)
+        nv = int(z["nv"])
+        return S.Problem(name=workload, views=[z[f"v{i}"] for i in range(nv)], weights=[z[f"w{i}"] for i in range(nv)],
+                         psfs=[z[f"p{i}"] for i in range(nv)], psftype=int(z["psftype"]),
+                         iterations=int(z["iterations"]), lam=float(z["lam"]), block=None)
+    prob = S.make_problem(cfg, shape_xyz=shape, psf_size_xyz=psf)
+    if path:
+        os.makedirs(cache, exist_ok=True)
+        arrs = {"nv": len(prob.views), "psftype": prob.psftype, "iterations": prob.iterations, "lam": prob.lam}
+        for i in range(len(prob.views)):
+            arrs[f"v{i}"], arrs[f"w{i}"], arrs[f"p{i}"] = prob.views[i], prob.weights[i], prob.psfs[i]
+        np.savez(path, **arrs)
+    return prob
 
 
 def bytes_per_iteration(dec, n_views, n_voxels):
@@ -137,8 +153,8 @@ def bytes_per_iteration(dec, n_views, n_voxels):
         Heff = nt * half * min(ez, tz)
         # forward plane: gather P reals, write H complex (x2 convolutions)
         out["plane_fwd"] += 2 * (4 * P + 8 * H)
-        # z pass: read H, read OTF H, write H (x2)
-        out["zpass"] += 2 * (24 * H)
+        # z pass: read H, write H, read the OTF once (all tiles of a view share its shape) (x2)
+        out["zpass"] += 2 * (16 * H + 8 * half * tz)
         # inverse plane: read effective spectrum slices; quotient reads img, writes q
         out["plane_inv_quotient"] += 8 * Heff + 8 * n_voxels
         # update reads psi, weight, writes psi

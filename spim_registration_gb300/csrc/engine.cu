@@ -2,6 +2,7 @@
 // and the small elementwise / reduction kernels of the deconvolution path.
 #include <algorithm>
 #include <atomic>
+#include <cstdlib>
 #include <cmath>
 #include <cstring>
 #include <sstream>
@@ -48,7 +49,7 @@ void DevBuf::ensure(size_t b) {
 
 bool is_smooth(int n) {
   if (n <= 0) return false;
-  for (int f : {2, 3, 5, 7})
+  for (int f : {2, 3, 5})
     while (n % f == 0) n /= f;
   return n == 1;
 }
@@ -62,7 +63,7 @@ int next_smooth(int n, bool even) {
 }
 
 // Radices of the register DFTs (fft_device.cuh).
-static const int kRadices[] = {16, 15, 14, 12, 10, 9, 8, 7, 6, 5, 4, 3, 2};
+static const int kRadices[] = {16, 15, 12, 10, 8, 6, 5, 4, 3, 2};
 
 static void best_split(int n, int depth, int maxdepth, std::vector<int>& cur, std::vector<int>& best) {
   if (n == 1) {
@@ -85,7 +86,7 @@ std::vector<int> factorize(int n) {
   if (n == 1) return {1};
   std::vector<int> cur, best;
   for (int depth = 1; depth <= kMaxStages && best.empty(); ++depth) best_split(n, 0, depth, cur, best);
-  if (best.empty()) throw std::invalid_argument("FFT length is not 2,3,5,7-smooth");
+  if (best.empty()) throw std::invalid_argument("FFT length is not 2,3,5-smooth");
   return best;
 }
 
@@ -186,6 +187,17 @@ void ConvPlan::upload() {
   up(d_items_z, items_z);
 }
 
+// Shared-memory budget of one plane buffer used by the planner (MVD_PLANE_CAP overrides it;
+// planes of at most half the budget let two CTAs share an SM).
+int plane_cap() {
+  static int cap = [] {
+    const char* e = std::getenv("MVD_PLANE_CAP");
+    int v = e ? std::atoi(e) : 0;
+    return (v >= 256 && v <= kPlaneCap) ? v : kPlaneCapDefault;
+  }();
+  return cap;
+}
+
 std::unique_ptr<ConvPlan> make_conv_plan(PlanTable& pt, int nx, int ny, int nz, int kx, int ky,
                                          int kz, const PlanOptions& opt) {
   if (nx < 1 || ny < 1 || nz < 1) throw std::invalid_argument("empty volume");
@@ -212,7 +224,7 @@ std::unique_ptr<ConvPlan> make_conv_plan(PlanTable& pt, int nx, int ny, int nz, 
   AxisTiles bx, by, bz;
   for (auto& a : ox)
     for (auto& b : oy) {
-      if ((long long)row_pitch(a.T / 2) * b.T > kPlaneCap) continue;
+      if ((long long)row_pitch(a.T / 2) * b.T > plane_cap()) continue;
       for (auto& c : oz) {
         const double ntiles = (double)a.n * b.n * c.n;
         const double cost = ntiles * a.T * b.T * c.T * (1.0 + 1e-3 * ntiles);

@@ -22,10 +22,10 @@ struct CudaError : std::runtime_error {
 void check_cuda(cudaError_t e, const char* what);
 #define MVD_CHECK(x) ::mvd::check_cuda((x), #x)
 
-// 2,3,5,7-smooth helpers
+// 2,3,5-smooth helpers (the FFT radices are products of 2, 3 and 5)
 bool is_smooth(int n);
 int next_smooth(int n, bool even);
-std::vector<int> factorize(int n);  // radices from {8,4,2,3,5,7}, product == n
+std::vector<int> factorize(int n);  // radices from {16,15,12,10,8,6,5,4,3,2}, product == n
 
 // Device memory owned by RAII
 struct DevBuf {
@@ -86,6 +86,9 @@ struct PlanOptions {
 // Choose tiles for a (volume, kernel) pair; effective regions cover the whole volume.
 std::unique_ptr<ConvPlan> make_conv_plan(PlanTable& pt, int nx, int ny, int nz, int kx, int ky,
                                          int kz, const PlanOptions& opt = PlanOptions());
+
+// Planner's budget for one plane buffer (complex values).
+int plane_cap();
 
 // Describe the plan for logs.
 std::string describe(const ConvPlan& p);

@@ -31,7 +31,7 @@ constexpr int kMaxStages = 6;
 struct FftPlan {
   int n;                    // transform length
   int nstages;              // number of radix stages
-  int radix[kMaxStages];    // radices (each in {2,3,4,5,6,7,8,9,10,12,14,15,16}), product == n
+  int radix[kMaxStages];    // radices (each in {2,3,4,5,6,8,10,12,15,16}), product == n
   const float2* tw;         // exp(-2 pi i k / n), k in [0, n)
   const float2* tw_r2c;     // for the real-input length 2n: exp(-2 pi i k / (2n)), k in [0, n]
 };
@@ -236,7 +236,23 @@ __device__ __forceinline__ void butterfly_index(int b, int count, int NR, int& b
   }
 }
 
-// One radix-R Stockham stage of `count` sequences: ld(batch, i) -> float2, st(batch, i, v).
+// Whole-butterfly access: a functor may define get<R>(batch, j, NR, v) (v[r] = element
+// j + r NR) and put<R>(batch, base, Ns, v) (element base + r Ns = v[r]) to batch its memory
+// operations; these defaults use the per-element operators.
+struct ElemAccess {
+  template <int R, class F>
+  __device__ __forceinline__ static void get(const F& f, int batch, int j, int NR, float2* v) {
+#pragma unroll
+    for (int r = 0; r < R; ++r) v[r] = f(batch, j + r * NR);
+  }
+  template <int R, class F>
+  __device__ __forceinline__ static void put(const F& f, int batch, int base, int Ns, const float2* v) {
+#pragma unroll
+    for (int r = 0; r < R; ++r) f(batch, base + r * Ns, v[r]);
+  }
+};
+
+// One radix-R Stockham stage of `count` sequences: ld.get<R>(...) and st.put<R>(...).
 template <int R, bool INV, bool JFAST, class LD, class ST>
 __device__ __forceinline__ void stage_r(int N, int Ns, int count, const float2* __restrict__ tw, const LD& ld,
                                         const ST& st) {
@@ -247,8 +263,7 @@ __device__ __forceinline__ void stage_r(int N, int Ns, int count, const float2* 
     int batch, j;
     butterfly_index<JFAST>(b, count, NR, batch, j);
     float2 v[R];
-#pragma unroll
-    for (int r = 0; r < R; ++r) v[r] = ld(batch, j + r * NR);
+    ld.template get<R>(batch, j, NR, v);
     const int k = j % Ns;
     if (k != 0) {
 #pragma unroll
@@ -259,9 +274,7 @@ __device__ __forceinline__ void stage_r(int N, int Ns, int count, const float2* 
       }
     }
     Dft<R, INV>::run(v);
-    const int base = (j - k) * R + k;
-#pragma unroll
-    for (int r = 0; r < R; ++r) st(batch, base + r * Ns, v[r]);
+    st.template put<R>(batch, (j - k) * R + k, Ns, v);
   }
 }
 
@@ -274,12 +287,9 @@ __device__ __forceinline__ void stage(int R, int N, int Ns, int count, const flo
     case 4: stage_r<4, INV, JFAST>(N, Ns, count, tw, ld, st); break;
     case 5: stage_r<5, INV, JFAST>(N, Ns, count, tw, ld, st); break;
     case 6: stage_r<6, INV, JFAST>(N, Ns, count, tw, ld, st); break;
-    case 7: stage_r<7, INV, JFAST>(N, Ns, count, tw, ld, st); break;
     case 8: stage_r<8, INV, JFAST>(N, Ns, count, tw, ld, st); break;
-    case 9: stage_r<9, INV, JFAST>(N, Ns, count, tw, ld, st); break;
     case 10: stage_r<10, INV, JFAST>(N, Ns, count, tw, ld, st); break;
     case 12: stage_r<12, INV, JFAST>(N, Ns, count, tw, ld, st); break;
-    case 14: stage_r<14, INV, JFAST>(N, Ns, count, tw, ld, st); break;
     case 15: stage_r<15, INV, JFAST>(N, Ns, count, tw, ld, st); break;
     case 16: stage_r<16, INV, JFAST>(N, Ns, count, tw, ld, st); break;
     default: stage_r<1, INV, JFAST>(N, Ns, count, tw, ld, st); break;  // length-1 transform: copy
@@ -298,18 +308,15 @@ __device__ __forceinline__ void zmid_r(int N, int count, const float2* __restric
     int batch, j;
     butterfly_index<false>(b, count, NR, batch, j);
     float2 v[R];
-#pragma unroll
-    for (int r = 0; r < R; ++r) v[r] = ld(batch, j + r * NR);
+    ld.template get<R>(batch, j, NR, v);
     if (j != 0) {
 #pragma unroll
       for (int r = 1; r < R; ++r) v[r] = cmul(v[r], __ldg(tw + r * j));
     }
     Dft<R, false>::run(v);
-#pragma unroll
-    for (int r = 0; r < R; ++r) v[r] = mul(batch, j + r * NR, v[r]);
+    mul.template apply<R>(batch, j, NR, v);
     Dft<R, true>::run(v);
-#pragma unroll
-    for (int r = 0; r < R; ++r) st(batch, j * R + r, v[r]);
+    st.template put<R>(batch, j * R, 1, v);
   }
 }
 
@@ -322,12 +329,9 @@ __device__ __forceinline__ void zmid(int R, int N, int count, const float2* __re
     case 4: zmid_r<4>(N, count, tw, ld, mul, st); break;
     case 5: zmid_r<5>(N, count, tw, ld, mul, st); break;
     case 6: zmid_r<6>(N, count, tw, ld, mul, st); break;
-    case 7: zmid_r<7>(N, count, tw, ld, mul, st); break;
     case 8: zmid_r<8>(N, count, tw, ld, mul, st); break;
-    case 9: zmid_r<9>(N, count, tw, ld, mul, st); break;
     case 10: zmid_r<10>(N, count, tw, ld, mul, st); break;
     case 12: zmid_r<12>(N, count, tw, ld, mul, st); break;
-    case 14: zmid_r<14>(N, count, tw, ld, mul, st); break;
     case 15: zmid_r<15>(N, count, tw, ld, mul, st); break;
     case 16: zmid_r<16>(N, count, tw, ld, mul, st); break;
     default: zmid_r<1>(N, count, tw, ld, mul, st); break;
@@ -335,13 +339,23 @@ __device__ __forceinline__ void zmid(int R, int N, int count, const float2* __re
 }
 
 // ---------------------------------------------------------------------------------------
-// Shared-memory accessor: element (batch, i) at p[batch * bs + i * es]
+// Shared-memory accessor: element (batch, i) at p[batch * bs + s(i) * es], where s(i) = i, or
+// i + i/16 for the skewed row layout (one type for every exchange keeps the code small).
 // ---------------------------------------------------------------------------------------
-struct SmemRef {
+struct Smem {
   float2* p;
-  int es, bs;
-  __device__ __forceinline__ float2 operator()(int batch, int i) const { return p[batch * bs + i * es]; }
-  __device__ __forceinline__ void operator()(int batch, int i, float2 v) const { p[batch * bs + i * es] = v; }
+  int es, bs, skew;
+  __device__ __forceinline__ int at(int batch, int i) const { return batch * bs + (i + ((i >> 4) & skew)) * es; }
+  __device__ __forceinline__ float2 operator()(int batch, int i) const { return p[at(batch, i)]; }
+  __device__ __forceinline__ void operator()(int batch, int i, float2 v) const { p[at(batch, i)] = v; }
+  template <int R>
+  __device__ __forceinline__ void get(int batch, int j, int NR, float2* v) const {
+    ElemAccess::get<R>(*this, batch, j, NR, v);
+  }
+  template <int R>
+  __device__ __forceinline__ void put(int batch, int base, int Ns, const float2* v) const {
+    ElemAccess::put<R>(*this, batch, base, Ns, v);
+  }
 };
 
 // ---------------------------------------------------------------------------------------

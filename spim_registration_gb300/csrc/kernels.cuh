@@ -21,9 +21,10 @@
 
 namespace mvd {
 
-constexpr int kThreads = 512;    // threads per CTA of the plane kernels
+constexpr int kThreads = 256;    // threads per CTA of the plane kernels (two CTAs fit an SM's registers)
 constexpr int kZThreads = 256;   // threads per CTA of the z-pencil kernel
 constexpr int kPlaneCap = 14336; // complex values of one shared-memory buffer (two are used)
+constexpr int kPlaneCapDefault = 7168;  // planner default: two CTAs per SM (measured faster)
 constexpr int kZChunk = 16;      // pencils per z-pass CTA (16 complex = one 128-byte line)
 constexpr int kZPitch = kZChunk + 1;
 
@@ -67,33 +68,54 @@ __device__ __forceinline__ int mirror_single(int i, int n) {
   return m < n ? m : period - m;
 }
 
+// Each gather resolves a row once (row(gy, gz)) and then reads x positions of that row.
 struct GatherMirror {  // psi extended mirror-single (MVDeconFFTThreads.java:44,78)
   VolumeRef v;
-  __device__ __forceinline__ float operator()(int gx, int gy, int gz) const {
-    gx = mirror_single(gx, v.nx);
-    gy = mirror_single(gy, v.ny);
-    gz = mirror_single(gz, v.nz);
-    return __ldg(v.data + ((long long)gz * v.ny + gy) * v.nx + gx);
+  struct Row {
+    const float* p;
+    int nx;
+    __device__ __forceinline__ float operator()(int gx) const { return __ldg(p + mirror_single(gx, nx)); }
+  };
+  __device__ __forceinline__ Row row(int gy, int gz) const {
+    return Row{v.data + ((long long)mirror_single(gz, v.nz) * v.ny + mirror_single(gy, v.ny)) * v.nx, v.nx};
   }
+  __device__ __forceinline__ float operator()(int gx, int gy, int gz) const { return row(gy, gz)(gx); }
 };
 
 struct GatherValue {  // quotient extended with a constant (value 1: MVDeconFFTThreads.java:63,103)
   VolumeRef v;
   float value;
-  __device__ __forceinline__ float operator()(int gx, int gy, int gz) const {
-    if (gx < 0 || gy < 0 || gz < 0 || gx >= v.nx || gy >= v.ny || gz >= v.nz) return value;
-    return __ldg(v.data + ((long long)gz * v.ny + gy) * v.nx + gx);
+  struct Row {
+    const float* p;  // nullptr: the whole row is outside the volume
+    int nx;
+    float value;
+    __device__ __forceinline__ float operator()(int gx) const {
+      return (p && gx >= 0 && gx < nx) ? __ldg(p + gx) : value;
+    }
+  };
+  __device__ __forceinline__ Row row(int gy, int gz) const {
+    const bool in = gy >= 0 && gz >= 0 && gy < v.ny && gz < v.nz;
+    return Row{in ? v.data + ((long long)gz * v.ny + gy) * v.nx : nullptr, v.nx, value};
   }
+  __device__ __forceinline__ float operator()(int gx, int gy, int gz) const { return row(gy, gz)(gx); }
 };
 
 // ------------------------------------------------------------------------------------------
-// epilogues of the inverse plane pass: called once per effective voxel, then finish()
+// epilogues of the inverse plane pass.  apply<K>(g0, off, val, ok) handles K voxels of one row
+// (global index g0 + off[i], value val[i], in the effective region if ok[i]): all loads are
+// issued before any store.  finish() ends the CTA's work (statistics).
 // ------------------------------------------------------------------------------------------
 struct EpiStore {
   float* out;
   int nx, ny;
   __device__ __forceinline__ void acc_init() {}
   __device__ __forceinline__ void operator()(long long g, float v) { out[g] = v; }
+  template <int K>
+  __device__ __forceinline__ void apply(long long g0, const int* off, const float* val, const bool* ok) {
+#pragma unroll
+    for (int i = 0; i < K; ++i)
+      if (ok[i]) out[g0 + off[i]] = val[i];
+  }
   __device__ __forceinline__ void finish() {}
 };
 
@@ -103,9 +125,22 @@ struct EpiQuotient {
   float* q;
   int nx, ny;
   __device__ __forceinline__ void acc_init() {}
-  __device__ __forceinline__ void operator()(long long g, float blurred) {
-    const float i = __ldg(img + g);
-    q[g] = i > 0.f ? __fdiv_rn(i, blurred) : 1.f;
+  __device__ __forceinline__ static float quotient(float i, float blurred) {
+    return i > 0.f ? __fdiv_rn(i, blurred) : 1.f;
+  }
+  __device__ __forceinline__ void operator()(long long g, float blurred) { q[g] = quotient(__ldg(img + g), blurred); }
+  template <int K>
+  __device__ __forceinline__ void apply(long long g0, const int* off, const float* val, const bool* ok) {
+    constexpr int C = K < 16 ? K : 16;
+#pragma unroll
+    for (int c = 0; c < K; c += C) {
+      float im[C];
+#pragma unroll
+      for (int i = 0; i < C; ++i) im[i] = (c + i < K && ok[c + i]) ? __ldg(img + g0 + off[c + i]) : 0.f;
+#pragma unroll
+      for (int i = 0; i < C; ++i)
+        if (c + i < K && ok[c + i]) q[g0 + off[c + i]] = quotient(im[i], val[c + i]);
+    }
   }
   __device__ __forceinline__ void finish() {}
 };
@@ -127,8 +162,7 @@ struct EpiUpdate {
     acc_sum = 0.f;
     acc_max = 0.f;
   }
-  __device__ __forceinline__ void operator()(long long g, float integral) {
-    const float last = psi[g];
+  __device__ __forceinline__ float next_value(float last, float integral, float w) {
     const float value = __fmul_rn(last, integral);
     float adjusted;
     if (value > 0.f) {
@@ -142,12 +176,30 @@ struct EpiUpdate {
       adjusted = 1e-4f;
     }
     const float next = isnan(adjusted) ? 1e-4f : fmaxf(1e-4f, adjusted);
-    const float w = __ldg(weight + g);
     const float out = __fadd_rn(last, __fmul_rn(__fsub_rn(next, last), w));
-    psi[g] = out;
     const float change = fabsf(__fsub_rn(out, last));
     acc_sum += change;
     acc_max = fmaxf(acc_max, change);
+    return out;
+  }
+  __device__ __forceinline__ void operator()(long long g, float integral) {
+    psi[g] = next_value(psi[g], integral, __ldg(weight + g));
+  }
+  template <int K>
+  __device__ __forceinline__ void apply(long long g0, const int* off, const float* val, const bool* ok) {
+    constexpr int C = K < 8 ? K : 8;  // voxels whose loads are in flight together
+#pragma unroll
+    for (int c = 0; c < K; c += C) {
+      float last[C], w[C];
+#pragma unroll
+      for (int i = 0; i < C; ++i) {
+        last[i] = (c + i < K && ok[c + i]) ? psi[g0 + off[c + i]] : 0.f;
+        w[i] = (c + i < K && ok[c + i]) ? __ldg(weight + g0 + off[c + i]) : 0.f;
+      }
+#pragma unroll
+      for (int i = 0; i < C; ++i)
+        if (c + i < K && ok[c + i]) psi[g0 + off[c + i]] = next_value(last[i], val[c + i], w[i]);
+    }
   }
   __device__ __forceinline__ void finish() {
     // FP64 block reduction of the per-thread partials, one atomic per CTA
@@ -186,91 +238,104 @@ struct EpiUpdate {
 // ------------------------------------------------------------------------------------------
 // load / store functors of the first and last FFT stages
 // ------------------------------------------------------------------------------------------
-// row element i of a row stored with the skew i + i/16 (used between row stages 0 and 1)
-struct SmemRowSkew {
-  float2* p;
-  int pitch;
-  __device__ __forceinline__ float2 operator()(int batch, int i) const { return p[batch * pitch + i + (i >> 4)]; }
-  __device__ __forceinline__ void operator()(int batch, int i, float2 v) const { p[batch * pitch + i + (i >> 4)] = v; }
-};
-
 template <class Gather>
 struct RowGather {  // packed pair (x[2n], x[2n+1]) of tile row `batch`, gathered from the volume
   Gather g;
   int ox, oy, gz;
-  __device__ __forceinline__ float2 operator()(int batch, int n) const {
-    const int gx = ox + 2 * n, gy = oy + batch;
-    return make_float2(g(gx, gy, gz), g(gx + 1, gy, gz));
+  template <int R>
+  __device__ __forceinline__ void get(int batch, int j, int NR, float2* v) const {
+    const auto row = g.row(oy + batch, gz);
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      const int gx = ox + 2 * (j + r * NR);
+      v[r] = make_float2(row(gx), row(gx + 1));
+    }
   }
 };
 
 struct SpecSliceLoad {  // spectrum slice [y][kx]: batch = kx, i = y
   const float2* p;
   int px;
-  __device__ __forceinline__ float2 operator()(int batch, int i) const { return __ldg(p + i * px + batch); }
+  template <int R>
+  __device__ __forceinline__ void get(int batch, int j, int NR, float2* v) const {
+#pragma unroll
+    for (int r = 0; r < R; ++r) v[r] = __ldg(p + (j + r * NR) * px + batch);
+  }
 };
 
 struct SpecSliceStore {
   float2* p;
   int px;
-  __device__ __forceinline__ void operator()(int batch, int i, float2 v) const { p[i * px + batch] = v; }
+  template <int R>
+  __device__ __forceinline__ void put(int batch, int base, int Ns, const float2* v) const {
+#pragma unroll
+    for (int r = 0; r < R; ++r) p[(base + r * Ns) * px + batch] = v[r];
+  }
 };
 
 struct PencilRef {  // pencil element: batch = pencil in the chunk, i = z
   float2* p;
   long long plane;
-  __device__ __forceinline__ float2 operator()(int batch, int i) const { return p[i * plane + batch]; }
-  __device__ __forceinline__ void operator()(int batch, int i, float2 v) const { p[i * plane + batch] = v; }
+  template <int R>
+  __device__ __forceinline__ void get(int batch, int j, int NR, float2* v) const {
+#pragma unroll
+    for (int r = 0; r < R; ++r) v[r] = p[(j + r * NR) * plane + batch];
+  }
+  template <int R>
+  __device__ __forceinline__ void put(int batch, int base, int Ns, const float2* v) const {
+#pragma unroll
+    for (int r = 0; r < R; ++r) p[(base + r * Ns) * plane + batch] = v[r];
+  }
 };
 
 struct PencilScaledStore {
   float2* p;
   long long plane;
   float scale;
-  __device__ __forceinline__ void operator()(int batch, int i, float2 v) const { p[i * plane + batch] = cscale(v, scale); }
+  template <int R>
+  __device__ __forceinline__ void put(int batch, int base, int Ns, const float2* v) const {
+#pragma unroll
+    for (int r = 0; r < R; ++r) p[(base + r * Ns) * plane + batch] = cscale(v[r], scale);
+  }
 };
 
-struct OtfMul {
+struct OtfMul {  // v[r] *= OTF at natural index j + r NR of pencil `batch`
   const float2* p;
   long long plane;
-  __device__ __forceinline__ float2 operator()(int batch, int k, float2 v) const {
-    return cmul(v, __ldg(p + k * plane + batch));
+  template <int R>
+  __device__ __forceinline__ void apply(int batch, int j, int NR, float2* v) const {
+    float2 o[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) o[r] = __ldg(p + (j + r * NR) * plane + batch);
+#pragma unroll
+    for (int r = 0; r < R; ++r) v[r] = cmul(v[r], o[r]);
   }
 };
 
 template <class Epi>
 struct RowEpilogue {  // last inverse x stage: complex n of effective row `batch` = reals 2n, 2n+1
   Epi* epi;
-  long long row0;     // global index of tile-local (x = 0, y = hy, z) in the volume
+  long long row0;     // global index of (tile-local x = hx, effective row 0, slice z)
   long long ystride;  // global stride of one row
   int hx, ex;
-  __device__ __forceinline__ void operator()(int batch, int n, float2 v) const {
-    const long long g = row0 + batch * ystride;
-    const int x0 = 2 * n - hx;
-    if (x0 >= 0 && x0 < ex) (*epi)(g + x0, v.x);
-    if (x0 + 1 >= 0 && x0 + 1 < ex) (*epi)(g + x0 + 1, v.y);
+  template <int R>
+  __device__ __forceinline__ void put(int batch, int base, int Ns, const float2* v) const {
+    int off[2 * R];
+    float val[2 * R];
+    bool ok[2 * R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      const int x0 = 2 * (base + r * Ns) - hx;
+      off[2 * r] = x0;
+      off[2 * r + 1] = x0 + 1;
+      val[2 * r] = v[r].x;
+      val[2 * r + 1] = v[r].y;
+      ok[2 * r] = x0 >= 0 && x0 < ex;
+      ok[2 * r + 1] = x0 + 1 >= 0 && x0 + 1 < ex;
+    }
+    epi->template apply<2 * R>(row0 + batch * ystride, off, val, ok);
   }
 };
-
-// Stage dispatch over the shared-memory layouts: `skew_in` / `skew_out` select the skewed
-// row layout (i + i/16) for the buffer read / written.
-template <bool INV, bool JFAST, class LD>
-__device__ __forceinline__ void stage_to_smem(int R, int n, int Ns, int count, const float2* tw, const LD& ld,
-                                              float2* dst, int es, int bs, bool skew_out) {
-  if (skew_out)
-    stage<INV, JFAST>(R, n, Ns, count, tw, ld, SmemRowSkew{dst, bs});
-  else
-    stage<INV, JFAST>(R, n, Ns, count, tw, ld, SmemRef{dst, es, bs});
-}
-
-template <bool INV, bool JFAST, class ST>
-__device__ __forceinline__ void stage_from_smem(int R, int n, int Ns, int count, const float2* tw, float2* src,
-                                                int es, int bs, bool skew_in, const ST& st) {
-  if (skew_in)
-    stage<INV, JFAST>(R, n, Ns, count, tw, SmemRowSkew{src, bs}, st);
-  else
-    stage<INV, JFAST>(R, n, Ns, count, tw, SmemRef{src, es, bs}, st);
-}
 
 // All stages of one transform with the result left in shared memory: on return (after a
 // barrier) `cur` holds it in the plain layout.  Stage 0 loads with ld0 (global memory or
@@ -285,15 +350,12 @@ __device__ __forceinline__ void run_transform_smem(const FftPlan* __restrict__ p
   int Ns = 1;
   for (int s = 0; s < ns; ++s) {
     const int R = __ldg(&p->radix[s]);
-    const bool skew_out = ROWS && s == 0 && ns > 1;
-    if (s == 0) {
-      stage_to_smem<INV, ROWS>(R, n, Ns, count, tw, ld0, oth, es, bs, skew_out);
-    } else {
-      if (ROWS && s == 1)
-        stage<INV, ROWS>(R, n, Ns, count, tw, SmemRowSkew{cur, bs}, SmemRef{oth, es, bs});
-      else
-        stage<INV, ROWS>(R, n, Ns, count, tw, SmemRef{cur, es, bs}, SmemRef{oth, es, bs});
-    }
+    const int skew_out = (ROWS && s == 0 && ns > 1) ? -1 : 0;
+    const int skew_in = (ROWS && s == 1) ? -1 : 0;
+    if (s == 0)
+      stage<INV, ROWS>(R, n, Ns, count, tw, ld0, Smem{oth, es, bs, skew_out});
+    else
+      stage<INV, ROWS>(R, n, Ns, count, tw, Smem{cur, es, bs, skew_in}, Smem{oth, es, bs, 0});
     __syncthreads();
     float2* t = cur;
     cur = oth;
@@ -317,16 +379,14 @@ __device__ __forceinline__ void run_transform_to(const FftPlan* __restrict__ p, 
   int Ns = 1;
   for (int s = 0; s < ns; ++s) {
     const int R = __ldg(&p->radix[s]);
-    const bool skew_in = ROWS && s == 1;
+    const int skew_in = (ROWS && s == 1) ? -1 : 0;
     if (s == ns - 1) {
-      stage_from_smem<INV, ROWS>(R, n, Ns, count, tw, cur, es, bs, skew_in, stl);
+      stage<INV, ROWS>(R, n, Ns, count, tw, Smem{cur, es, bs, skew_in}, stl);
     } else {
       if (s == 0)
-        stage_to_smem<INV, ROWS>(R, n, Ns, count, tw, ld0, oth, es, bs, ROWS);
-      else if (skew_in)
-        stage<INV, ROWS>(R, n, Ns, count, tw, SmemRowSkew{cur, bs}, SmemRef{oth, es, bs});
+        stage<INV, ROWS>(R, n, Ns, count, tw, ld0, Smem{oth, es, bs, ROWS ? -1 : 0});
       else
-        stage<INV, ROWS>(R, n, Ns, count, tw, SmemRef{cur, es, bs}, SmemRef{oth, es, bs});
+        stage<INV, ROWS>(R, n, Ns, count, tw, Smem{cur, es, bs, skew_in}, Smem{oth, es, bs, 0});
       __syncthreads();
       float2* t = cur;
       cur = oth;
@@ -337,10 +397,10 @@ __device__ __forceinline__ void run_transform_to(const FftPlan* __restrict__ p, 
 }
 
 // ------------------------------------------------------------------------------------------
-// kernels (templated on gather / epilogue; instantiated in engine.cu)
+// kernels (templated on gather / epilogue; instantiated in passes_*.cu)
 // ------------------------------------------------------------------------------------------
 template <class Gather>
-__global__ void __launch_bounds__(kThreads, 1)
+__global__ void __launch_bounds__(kThreads, 2)
 plane_fwd_kernel(const TileDesc* __restrict__ tiles, const int2* __restrict__ items,
                  const FftPlan* __restrict__ plans, float2* __restrict__ spec, Gather gather) {
   extern __shared__ float2 sm[];
@@ -358,11 +418,11 @@ plane_fwd_kernel(const TileDesc* __restrict__ tiles, const int2* __restrict__ it
   __syncthreads();
   // y: C2C of every column, last stage straight to the spectrum slice
   SpecSliceStore st{spec + t.spec_off + (long long)z * t.ty * t.px, t.px};
-  run_transform_to<false, false>(plans + t.plan_y, t.px, SmemRef{cur, t.pitch, 1}, st, cur, oth, t.pitch, 1);
+  run_transform_to<false, false>(plans + t.plan_y, t.px, Smem{cur, t.pitch, 1, 0}, st, cur, oth, t.pitch, 1);
 }
 
 template <class Epi>
-__global__ void __launch_bounds__(kThreads, 1)
+__global__ void __launch_bounds__(kThreads, 2)
 plane_inv_kernel(const TileDesc* __restrict__ tiles, const int2* __restrict__ items,
                  const FftPlan* __restrict__ plans, const float2* __restrict__ spec, Epi epi) {
   extern __shared__ float2 sm[];
@@ -384,13 +444,14 @@ plane_inv_kernel(const TileDesc* __restrict__ tiles, const int2* __restrict__ it
   RowEpilogue<Epi> st{&epi, (gz * epi.ny + (t.oy + t.hy)) * (long long)epi.nx + t.ox + t.hx, (long long)epi.nx,
                       t.hx, t.ex};
   epi.acc_init();
-  run_transform_to<true, true>(plans + t.plan_x, t.ey, SmemRef{rows, 1, t.pitch}, st, rows, rows_oth, 1, t.pitch);
+  run_transform_to<true, true>(plans + t.plan_x, t.ey, Smem{rows, 1, t.pitch, 0}, st, rows, rows_oth, 1, t.pitch);
   epi.finish();
 }
 
 // MODE 0: forward z, multiply by the OTF, inverse z.  MODE 1: forward z and scale (OTF build).
-template <int MODE>
-__global__ void __launch_bounds__(kZThreads)
+// OCC: CTAs per SM the register allocation is sized for.
+template <int MODE, int OCC = 2>
+__global__ void __launch_bounds__(kZThreads, OCC)
 zpass_kernel(const TileDesc* __restrict__ tiles, const int2* __restrict__ items,
              const FftPlan* __restrict__ plans, float2* __restrict__ spec,
              const float2* __restrict__ otf, float scale) {
@@ -421,9 +482,9 @@ zpass_kernel(const TileDesc* __restrict__ tiles, const int2* __restrict__ items,
   for (int s = 0; s < ns - 1; ++s) {
     const int R = __ldg(&pz->radix[s]);
     if (s == 0) {
-      stage<false, false>(R, n, Ns, count, tw, g, SmemRef{cur, kZPitch, 1});
+      stage<false, false>(R, n, Ns, count, tw, g, Smem{cur, kZPitch, 1, 0});
     } else {
-      stage<false, false>(R, n, Ns, count, tw, SmemRef{cur, kZPitch, 1}, SmemRef{oth, kZPitch, 1});
+      stage<false, false>(R, n, Ns, count, tw, Smem{cur, kZPitch, 1, 0}, Smem{oth, kZPitch, 1, 0});
       float2* tmp = cur;
       cur = oth;
       oth = tmp;
@@ -432,7 +493,7 @@ zpass_kernel(const TileDesc* __restrict__ tiles, const int2* __restrict__ items,
     Ns *= R;
   }
   // forward last stage, product with the OTF, inverse first stage
-  zmid(__ldg(&pz->radix[ns - 1]), n, count, tw, SmemRef{cur, kZPitch, 1}, mul, SmemRef{oth, kZPitch, 1});
+  zmid(__ldg(&pz->radix[ns - 1]), n, count, tw, Smem{cur, kZPitch, 1, 0}, mul, Smem{oth, kZPitch, 1, 0});
   __syncthreads();
   {
     float2* tmp = cur;
@@ -444,9 +505,9 @@ zpass_kernel(const TileDesc* __restrict__ tiles, const int2* __restrict__ items,
   for (int i = 1; i < ns; ++i) {
     const int R = __ldg(&pz->radix[ns - 1 - i]);
     if (i == ns - 1) {
-      stage<true, false>(R, n, Ns, count, tw, SmemRef{cur, kZPitch, 1}, g);
+      stage<true, false>(R, n, Ns, count, tw, Smem{cur, kZPitch, 1, 0}, g);
     } else {
-      stage<true, false>(R, n, Ns, count, tw, SmemRef{cur, kZPitch, 1}, SmemRef{oth, kZPitch, 1});
+      stage<true, false>(R, n, Ns, count, tw, Smem{cur, kZPitch, 1, 0}, Smem{oth, kZPitch, 1, 0});
       __syncthreads();
       float2* tmp = cur;
       cur = oth;
