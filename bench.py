@@ -162,6 +162,23 @@ def bytes_per_iteration(dec, n_views, n_voxels):
     return out
 
 
+def max_over_ranks(ms: float, world: int) -> float:
+    """Slowest rank's timed region (ms); every rank gets the same value."""
+    if world <= 1:
+        return ms
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([ms], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_value(units_per_rank: float, ms_max: float, world: int) -> float:
+    """Whole-job throughput of `world` independent replicas: all ranks' units / the max time."""
+    return units_per_rank * world / (ms_max / 1e3)
+
+
 def run_ours(args, rank, world, local):
     import torch
 
@@ -208,13 +225,9 @@ def run_ours(args, rank, world, local):
     ms = e0.elapsed_time(e1)
     clock_info = clocks.stop()
     launches = dec.launch_count() - launches0
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([ms], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(ms, world)
     ms_per_step = ms / args.steps
-    value = n_vox * V * args.steps * world / (ms / 1e3)
+    value = replica_value(n_vox * V * args.steps, ms, world)
 
     # per-pass device time (CUDA events on the library's stream) for the roofline
     prof = dec.profile_iteration()
