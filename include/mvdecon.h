@@ -152,6 +152,20 @@ int mvd_get_launch_count(mvd_decon* h, long long* launches);
  * launches[k] the number of launches of each kind. */
 int mvd_profile_iteration(mvd_decon* h, double* ms, int* launches);
 
+/* ----- forward / backward of the multiview Poisson image-formation model -----
+ * No counterpart in the reference (its Java code has no gradients); the pair that PSF
+ * refinement from bead data needs, the analogue of a torch.autograd.Function:
+ *   f_v = ext(psi) (*) kernel1_v        (mirror-single extension, as in the first convolution)
+ *   NLL = sum_v sum_{x: img_v > 0} w_v (f_v - img_v log f_v)
+ * mvd_forward returns NLL (FP64 sum).  mvd_backward writes dNLL/dpsi (N floats) and
+ * dNLL/dkernel1_v (psf-sized, one buffer per view); each view's blur is recomputed tile by
+ * tile instead of being kept.  Fused handles only (not MVD_FLAG_PLAIN). */
+int mvd_forward(mvd_decon* h, double* nll);
+int mvd_backward(mvd_decon* h, float* grad_psi, float* const* grad_psf);
+/* Replace kernel1 (the PSF used by the first convolution and the model) or kernel2 of a view,
+ * as given (no normalisation), and its spectra -- e.g. after a projected gradient step. */
+int mvd_set_kernel(mvd_decon* h, int view, int which /* 1 or 2 */, const float* data);
+
 #ifdef __cplusplus
 }
 #endif

@@ -396,16 +396,64 @@ def deconvolve(problem, iterations=None, arith="f64", block="problem", quirk_thr
 
 
 # --------------------------------------------------------------------------------------------
-# image-formation model (adjoint pair checker)
+# image-formation model and its gradients (checker of the forward/backward pair)
 # --------------------------------------------------------------------------------------------
 def poisson_nll(psi, views, weights, psfs):
-    """NLL(psi, P) = sum_v sum_x w_v [f_v - img_v log f_v] over img_v > 0, f_v = ext(psi) (*) P_v.
+    """NLL(psi, P) = sum_v sum_{x: img_v > 0} w_v [f_v - img_v log f_v],  f_v = ext(psi) (*) P_v.
 
-    Psfs are used as given (no normalisation); FP64.
+    ext is the mirror-single extension of the first convolution of an iteration
+    (MVDeconFFTThreads.java:44,78); the PSFs are used as given; FP64.
     """
     total = 0.0
     for img, w, p in zip(views, weights, psfs):
-        f = conv_extended(psi, p, MIRROR, 0.0, "f64")
+        f = conv_extended(np.asarray(psi, dtype=np.float64), p, MIRROR, 0.0, "f64")
         m = img > 0
         total += math.fsum((w[m].astype(np.float64) * (f[m] - img[m].astype(np.float64) * np.log(f[m]))).ravel())
     return total
+
+
+def fold_mirror(c: np.ndarray, n_shape, h):
+    """Adjoint of the mirror-single extension: c lives on [-h, n+h) per axis; every extended
+    position adds into the voxel it mirrors."""
+    out = c
+    for axis in range(3):
+        n, hh = n_shape[axis], h[axis]
+        idx = mirror_single_index(np.arange(-hh, n + hh), n)
+        moved = np.moveaxis(out, axis, 0)
+        acc = np.zeros((n,) + moved.shape[1:], dtype=np.float64)
+        np.add.at(acc, idx, moved)
+        out = np.moveaxis(acc, 0, axis)
+    return out
+
+
+def poisson_nll_grad(psi, views, weights, psfs):
+    """Analytic gradients of poisson_nll w.r.t. psi and every PSF voxel (FP64).
+
+    r_v = w_v (1 - img_v / f_v) on img_v > 0 (else 0);
+    dNLL/dpsi   = sum_v fold( r_v (zero-extended) (*) mirror(P_v) on [-h, n+h) );
+    dNLL/dP_v(j) = sum_x r_v(x) ext(psi)(x - (j - k/2)).
+    """
+    psi = np.asarray(psi, dtype=np.float64)
+    g_psi = np.zeros_like(psi)
+    g_psf = []
+    for img, w, p in zip(views, weights, psfs):
+        p = np.asarray(p, dtype=np.float64)
+        f = conv_extended(psi, p, MIRROR, 0.0, "f64")
+        m = img > 0
+        r = np.where(m, w.astype(np.float64) * (1.0 - img.astype(np.float64) / np.where(m, f, 1.0)), 0.0)
+        h = [s // 2 for s in p.shape]
+        r_ext = extend(r, h, h, VALUE, 0.0)
+        c = conv_extended(r_ext, mirror(p), VALUE, 0.0, "f64")
+        g_psi += fold_mirror(c, psi.shape, h)
+        hi = [s - 1 - s // 2 for s in p.shape]
+        pe = extend(psi, h, hi, MIRROR)  # pe[u + h] = ext(psi)(u), u in [-h, n + hi)
+        nz, ny, nx = psi.shape
+        g = np.zeros(p.shape)
+        for jz in range(p.shape[0]):
+            for jy in range(p.shape[1]):
+                for jx in range(p.shape[2]):
+                    # ext(psi)(x - (j - h)) = pe[x - j + 2h]
+                    oz, oy, ox = 2 * h[0] - jz, 2 * h[1] - jy, 2 * h[2] - jx
+                    g[jz, jy, jx] = np.sum(r * pe[oz:oz + nz, oy:oy + ny, ox:ox + nx])
+        g_psf.append(g)
+    return g_psi, g_psf

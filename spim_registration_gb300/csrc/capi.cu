@@ -347,6 +347,17 @@ struct mvd_decon {
     if (stream) cudaStreamDestroy(stream);
   }
 
+  // forward/backward of the image-formation model (allocated on first use)
+  struct AdjView {
+    std::unique_ptr<ConvPlan> ext;   // plan over the volume extended by k/2 (tiles shifted by -k/2)
+    DevBuf otf_m;                    // spectrum of mirror(kernel1) on `ext`
+    DevBuf fold_tab;                 // CSR tables of the mirror fold
+    DevBuf lag_tile, lag_items_z, lag_items_inv;  // one full tile of the view's plan
+    int n_lag_z = 0, n_lag_inv = 0;
+  };
+  std::vector<AdjView> adj;
+  DevBuf r, c_ext, spec_ext, spec_b, acc, lag_real, g_psi, g_psf, d_nll;
+
   StatSlot* slot(int v) { return stats.as<StatSlot>() + v; }
 
   void enqueue_view(int v) {
@@ -831,6 +842,183 @@ extern "C" int mvd_profile_iteration(mvd_decon* h, double* ms, int* launches) {
   for (auto e : ev) cudaEventDestroy(e);
   ++h->iteration;
   h->launches += 6 * h->V + h->V + 1;
+  return MVD_OK;
+  MVD_API_END
+}
+
+// =========================================================================================
+// forward / backward pair of the multiview Poisson image-formation model
+// (no counterpart in the reference: gradients for PSF refinement from bead data)
+// =========================================================================================
+namespace {
+
+void adjoint_setup(mvd_decon* h) {
+  if (!h->adj.empty()) return;
+  h->adj.resize(h->V);
+  long long ext_max = 0, spec_ext_max = 0, tile_max = 0, otf_max = 0;
+  for (int v = 0; v < h->V; ++v) {
+    mvd_decon::AdjView& a = h->adj[v];
+    const auto& k = h->kd[v];
+    const int hx = k[0] / 2, hy = k[1] / 2, hz = k[2] / 2;
+    const int nxe = h->dims[0] + 2 * hx, nye = h->dims[1] + 2 * hy, nze = h->dims[2] + 2 * hz;
+    a.ext = make_conv_plan(h->pt, nxe, nye, nze, k[0], k[1], k[2]);
+    for (auto& t : a.ext->tiles) {  // tile coordinates in the original volume's frame
+      t.ox -= hx;
+      t.oy -= hy;
+      t.oz -= hz;
+    }
+    a.ext->upload();
+    ext_max = std::max(ext_max, (long long)nxe * nye * nze);
+    spec_ext_max = std::max(spec_ext_max, a.ext->spec_elems);
+    DevBuf mk = mirrored(h, h->k1[v].as<float>(), k);
+    a.otf_m.alloc(a.ext->otf_elems * sizeof(float2));
+    build_otf(h->pt, *a.ext, mk.as<float>(), a.otf_m.as<float2>(), h->scratch, h->stream);
+    std::vector<int> tab, st, ix;
+    const int n3[3] = {h->dims[0], h->dims[1], h->dims[2]}, h3[3] = {hx, hy, hz};
+    for (int d = 0; d < 3; ++d) {
+      mirror_fold_table(n3[d], h3[d], st, ix);
+      tab.insert(tab.end(), st.begin(), st.end());
+      tab.insert(tab.end(), ix.begin(), ix.end());
+    }
+    a.fold_tab.alloc(tab.size() * sizeof(int));
+    MVD_CHECK(cudaMemcpy(a.fold_tab.p, tab.data(), tab.size() * sizeof(int), cudaMemcpyHostToDevice));
+    // one full tile of the view's plan, for the inverse transform of the accumulated spectrum
+    const ConvPlan& p = *h->plans[v];
+    TileDesc t = p.tiles[0];
+    t.ox = t.oy = t.oz = 0;
+    t.hx = t.hy = t.hz = 0;
+    t.ex = p.ax.T;
+    t.ey = p.ay.T;
+    t.ez = p.az.T;
+    t.spec_off = 0;
+    t.otf_off = 0;
+    std::vector<int2> iz, ii;
+    for (int p0 = 0; p0 < t.ty * t.px; p0 += kZChunk) iz.push_back(make_int2(0, p0));
+    for (int z = 0; z < t.tz; ++z) ii.push_back(make_int2(0, z));
+    a.lag_tile.alloc(sizeof(TileDesc));
+    a.lag_items_z.alloc(iz.size() * sizeof(int2));
+    a.lag_items_inv.alloc(ii.size() * sizeof(int2));
+    MVD_CHECK(cudaMemcpy(a.lag_tile.p, &t, sizeof(TileDesc), cudaMemcpyHostToDevice));
+    MVD_CHECK(cudaMemcpy(a.lag_items_z.p, iz.data(), iz.size() * sizeof(int2), cudaMemcpyHostToDevice));
+    MVD_CHECK(cudaMemcpy(a.lag_items_inv.p, ii.data(), ii.size() * sizeof(int2), cudaMemcpyHostToDevice));
+    a.n_lag_z = (int)iz.size();
+    a.n_lag_inv = (int)ii.size();
+    tile_max = std::max(tile_max, (long long)p.ax.T * p.ay.T * p.az.T);
+    otf_max = std::max(otf_max, p.otf_elems);
+  }
+  long long spec_max = 0, kmax = 0;
+  for (int v = 0; v < h->V; ++v) {
+    spec_max = std::max(spec_max, h->plans[v]->spec_elems);
+    kmax = std::max(kmax, vox(h->kd[v]));
+  }
+  h->r.alloc(h->N * sizeof(float));
+  h->c_ext.alloc(ext_max * sizeof(float));
+  h->spec_ext.alloc(spec_ext_max * sizeof(float2));
+  h->spec_b.alloc(spec_max * sizeof(float2));
+  h->acc.alloc(otf_max * sizeof(float2));
+  h->lag_real.alloc(tile_max * sizeof(float));
+  h->g_psi.alloc(h->N * sizeof(float));
+  h->g_psf.alloc(kmax * sizeof(float));
+  h->d_nll.alloc(sizeof(double));
+  MVD_CHECK(cudaStreamSynchronize(h->stream));
+}
+
+// f_v = ext(psi) (*) kernel1_v; NLL epilogue (residual into h->r when `residual`)
+void enqueue_blur_nll(mvd_decon* h, int v, bool residual) {
+  const ConvPlan& p = *h->plans[v];
+  float2* sp = h->spec.as<float2>();
+  launch_fwd_mirror(h->pt, p, h->psi.as<float>(), sp, h->stream);
+  launch_z(h->pt, p, sp, h->otf1[v].as<float2>(), h->stream);
+  launch_inv_nll(h->pt, p, sp, h->img[v].as<float>(), h->w[v].as<float>(), residual ? h->r.as<float>() : nullptr,
+                 h->d_nll.as<double>(), h->stream);
+}
+
+}  // namespace
+
+extern "C" int mvd_forward(mvd_decon* h, double* nll) {
+  MVD_API_BEGIN
+  if (!h || !nll) return fail(MVD_ERR_ARG, "NULL argument");
+  if (h->flags & MVD_FLAG_PLAIN) return fail(MVD_ERR_STATE, "forward/backward need the fused form");
+  MVD_CHECK(cudaSetDevice(h->dev));
+  adjoint_setup(h);
+  MVD_CHECK(cudaMemsetAsync(h->d_nll.p, 0, sizeof(double), h->stream));
+  for (int v = 0; v < h->V; ++v) enqueue_blur_nll(h, v, false);
+  MVD_CHECK(cudaMemcpyAsync(nll, h->d_nll.p, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  MVD_CHECK(cudaStreamSynchronize(h->stream));
+  return MVD_OK;
+  MVD_API_END
+}
+
+extern "C" int mvd_backward(mvd_decon* h, float* grad_psi, float* const* grad_psf) {
+  MVD_API_BEGIN
+  if (!h || !grad_psi || !grad_psf) return fail(MVD_ERR_ARG, "NULL argument");
+  if (h->flags & MVD_FLAG_PLAIN) return fail(MVD_ERR_STATE, "forward/backward need the fused form");
+  for (int v = 0; v < h->V; ++v)
+    if (!grad_psf[v]) return fail(MVD_ERR_ARG, "NULL PSF gradient buffer");
+  MVD_CHECK(cudaSetDevice(h->dev));
+  adjoint_setup(h);
+  cudaStream_t s = h->stream;
+  MVD_CHECK(cudaMemsetAsync(h->g_psi.p, 0, h->N * sizeof(float), s));
+  MVD_CHECK(cudaMemsetAsync(h->d_nll.p, 0, sizeof(double), s));
+  for (int v = 0; v < h->V; ++v) {
+    const ConvPlan& p = *h->plans[v];
+    mvd_decon::AdjView& a = h->adj[v];
+    const auto& k = h->kd[v];
+    // recompute this view's blur and residual (no blurred view is kept between calls)
+    enqueue_blur_nll(h, v, true);
+    // dNLL/dpsi: residual (zero outside) convolved with mirror(kernel1) on the extended grid,
+    // then folded back through the mirror-single extension
+    const ConvPlan& e = *a.ext;
+    float2* se = h->spec_ext.as<float2>();
+    launch_fwd_value_items(h->pt, e, e.d_tiles.as<TileDesc>(), e.d_items_fwd.as<int2>(), (int)e.items_fwd.size(),
+                           h->r.as<float>(), h->dims[0], h->dims[1], h->dims[2], 0.f, se, s);
+    launch_z(h->pt, e, se, a.otf_m.as<float2>(), s);
+    const long long off = ((long long)(k[2] / 2) * e.ny + k[1] / 2) * e.nx + k[0] / 2;
+    launch_inv_store_items(h->pt, e, e.d_tiles.as<TileDesc>(), e.d_items_inv.as<int2>(), (int)e.items_inv.size(),
+                           se, h->c_ext.as<float>() + off, e.nx, e.ny, s);
+    dev_fold_mirror(h->c_ext.as<float>(), e.nx, e.ny, a.fold_tab.as<int>(), h->dims[0], h->dims[1], h->dims[2],
+                    h->g_psi.as<float>(), s);
+    // dNLL/dP_v(j) = sum_x r(x) ext(psi)(x - (j - k/2)): per tile, spectrum of the residual
+    // restricted to the effective region times the conjugate spectrum of ext(psi) over the
+    // tile window, summed over tiles; one inverse transform; the kernel-sized lags
+    float2* sa = h->spec.as<float2>();
+    float2* sb = h->spec_b.as<float2>();
+    launch_fwd_mirror(h->pt, p, h->psi.as<float>(), sa, s);
+    launch_z_forward(h->pt, p, sa, s);
+    launch_fwd_masked(h->pt, p, h->r.as<float>(), sb, s);
+    launch_z_forward(h->pt, p, sb, s);
+    dev_cross_accumulate(sb, sa, (int)p.tiles.size(), p.otf_elems, h->acc.as<float2>(), s);
+    launch_z_inverse_items(h->pt, p, a.lag_tile.as<TileDesc>(), a.lag_items_z.as<int2>(), a.n_lag_z,
+                           h->acc.as<float2>(), s);
+    launch_inv_store_items(h->pt, p, a.lag_tile.as<TileDesc>(), a.lag_items_inv.as<int2>(), a.n_lag_inv,
+                           h->acc.as<float2>(), h->lag_real.as<float>(), p.ax.T, p.ay.T, s);
+    const double n_tile = (double)p.ax.T * p.ay.T * p.az.T;
+    dev_extract_lags(h->lag_real.as<float>(), p.ax.T, p.ay.T, p.az.T, k[0], k[1], k[2], (float)(1.0 / n_tile),
+                     h->g_psf.as<float>(), s);
+    MVD_CHECK(cudaMemcpyAsync(grad_psf[v], h->g_psf.p, vox(k) * sizeof(float), cudaMemcpyDeviceToHost, s));
+  }
+  MVD_CHECK(cudaMemcpyAsync(grad_psi, h->g_psi.p, h->N * sizeof(float), cudaMemcpyDeviceToHost, s));
+  MVD_CHECK(cudaStreamSynchronize(s));
+  return MVD_OK;
+  MVD_API_END
+}
+
+extern "C" int mvd_set_kernel(mvd_decon* h, int view, int which, const float* data) {
+  MVD_API_BEGIN
+  if (!h || !data) return fail(MVD_ERR_ARG, "NULL argument");
+  if (view < 0 || view >= h->V || (which != 1 && which != 2)) return fail(MVD_ERR_ARG, "bad view or kernel");
+  MVD_CHECK(cudaSetDevice(h->dev));
+  DevBuf& k = which == 1 ? h->k1[view] : h->k2[view];
+  MVD_CHECK(cudaMemcpyAsync(k.p, data, vox(h->kd[view]) * sizeof(float), cudaMemcpyHostToDevice, h->stream));
+  const ConvPlan& p = *h->plans[view];
+  build_otf(h->pt, p, k.as<float>(), (which == 1 ? h->otf1[view] : h->otf2[view]).as<float2>(), h->scratch,
+            h->stream);
+  if (which == 1 && !h->adj.empty()) {
+    mvd_decon::AdjView& a = h->adj[view];
+    DevBuf mk = mirrored(h, h->k1[view].as<float>(), h->kd[view]);
+    build_otf(h->pt, *a.ext, mk.as<float>(), a.otf_m.as<float2>(), h->scratch, h->stream);
+  }
+  MVD_CHECK(cudaStreamSynchronize(h->stream));
   return MVD_OK;
   MVD_API_END
 }

@@ -134,6 +134,32 @@ void launch_inv_update(PlanTable& pt, const ConvPlan& p, const float2* spec, flo
 long long launch_count();
 void count_launch(int n = 1);
 
+// ---- forward/backward of the Poisson image-formation model (adjoint.cu, passes_*.cu) ----
+// forward plane pass of `vol` (value 0 outside) keeping only each tile's effective region
+void launch_fwd_masked(PlanTable& pt, const ConvPlan& p, const float* vol, float2* spec, cudaStream_t s);
+// forward-only z pass (unscaled) over every tile of p
+void launch_z_forward(PlanTable& pt, const ConvPlan& p, float2* spec, cudaStream_t s);
+// inverse-only z pass over explicit tables
+void launch_z_inverse_items(PlanTable& pt, const ConvPlan& p, const TileDesc* tiles, const int2* items, int nitems,
+                            float2* spec, cudaStream_t s);
+// inverse plane pass storing the effective region of explicit tiles into out (dims nx, ny)
+void launch_inv_store_items(PlanTable& pt, const ConvPlan& p, const TileDesc* tiles, const int2* items, int nitems,
+                            const float2* spec, float* out, int nx, int ny, cudaStream_t s);
+// inverse plane pass with the NLL epilogue: nll += sum, r = residual (r may be null)
+void launch_inv_nll(PlanTable& pt, const ConvPlan& p, const float2* spec, const float* img, const float* w, float* r,
+                    double* nll, cudaStream_t s);
+// acc[i] = sum_t B_t[i] conj(A_t[i]) over `ntiles` tile spectra of `elems` values each
+void dev_cross_accumulate(const float2* B, const float2* A, int ntiles, long long elems, float2* acc, cudaStream_t s);
+// G[j] = scale * R[(j - k/2) mod T] for the kernel-sized output G (circular lags of a tile)
+void dev_extract_lags(const float* R, int tx, int ty, int tz, int kx, int ky, int kz, float scale, float* G,
+                      cudaStream_t s);
+// g[y] += sum of c over the extended positions that mirror-single maps to y; the tables list,
+// per axis, for each y in [0, n) the extended indices (CSR: start[n + 1], idx[]).
+void dev_fold_mirror(const float* c, int nxe, int nye, const int* tab, int nx, int ny, int nz, float* g,
+                     cudaStream_t s);
+// host: CSR tables of the mirror fold for an axis of n voxels extended by h on both sides
+void mirror_fold_table(int n, int h, std::vector<int>& start, std::vector<int>& idx);
+
 // ---- elementwise / reduction helpers (misc kernels) ----
 void dev_sum_f64(const float* x, long long n, double* out_dev, cudaStream_t s);  // *out += sum
 void dev_scale_div(float* x, long long n, const double* div_dev, cudaStream_t s); // x = (float)(x / d)

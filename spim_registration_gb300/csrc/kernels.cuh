@@ -235,20 +235,92 @@ struct EpiUpdate {
   }
 };
 
+// Poisson negative log-likelihood of the image-formation model and its residual:
+// for img > 0: nll += w (f - img log f), r = w (1 - img / f); else r = 0.
+// The per-thread partial sums are float; the CTA reduction and the global sum are FP64.
+struct EpiNll {
+  const float* img;
+  const float* weight;
+  float* r;           // residual out (may be null)
+  double* nll;        // += sum over the CTA's voxels
+  int nx, ny;
+  float acc;
+  __device__ __forceinline__ void acc_init() { acc = 0.f; }
+  __device__ __forceinline__ float term(float f, float im, float w, float& res) {
+    if (im > 0.f) {
+      res = __fmul_rn(w, __fsub_rn(1.f, __fdiv_rn(im, f)));
+      return w * (f - im * logf(f));
+    }
+    res = 0.f;
+    return 0.f;
+  }
+  __device__ __forceinline__ void operator()(long long g, float f) {
+    float res;
+    acc += term(f, __ldg(img + g), __ldg(weight + g), res);
+    if (r) r[g] = res;
+  }
+  template <int K>
+  __device__ __forceinline__ void apply(long long g0, const int* off, const float* val, const bool* ok) {
+    constexpr int C = K < 8 ? K : 8;
+#pragma unroll
+    for (int c = 0; c < K; c += C) {
+      float im[C], w[C];
+#pragma unroll
+      for (int i = 0; i < C; ++i) {
+        im[i] = (c + i < K && ok[c + i]) ? __ldg(img + g0 + off[c + i]) : 0.f;
+        w[i] = (c + i < K && ok[c + i]) ? __ldg(weight + g0 + off[c + i]) : 0.f;
+      }
+#pragma unroll
+      for (int i = 0; i < C; ++i) {
+        if (c + i < K && ok[c + i]) {
+          float res;
+          acc += term(val[c + i], im[i], w[i], res);
+          if (r) r[g0 + off[c + i]] = res;
+        }
+      }
+    }
+  }
+  __device__ __forceinline__ void finish() {
+    __shared__ double red[32];
+    double sum = (double)acc;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0) red[warp] = sum;
+    __syncthreads();
+    if (warp == 0) {
+      sum = lane < (int)(blockDim.x >> 5) ? red[lane] : 0.0;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+      if (lane == 0) atomicAdd(nll, sum);
+    }
+  }
+};
+
 // ------------------------------------------------------------------------------------------
 // load / store functors of the first and last FFT stages
 // ------------------------------------------------------------------------------------------
-template <class Gather>
+template <class Gather, bool MASK = false>
 struct RowGather {  // packed pair (x[2n], x[2n+1]) of tile row `batch`, gathered from the volume
   Gather g;
   int ox, oy, gz;
+  // MASK: values outside the tile's effective region [x0, x1) x [y0, y1) (slice inside: zin)
+  int x0, x1, y0, y1;
+  bool zin;
   template <int R>
   __device__ __forceinline__ void get(int batch, int j, int NR, float2* v) const {
     const auto row = g.row(oy + batch, gz);
+    const bool yin = !MASK || (zin && batch >= y0 && batch < y1);
 #pragma unroll
     for (int r = 0; r < R; ++r) {
-      const int gx = ox + 2 * (j + r * NR);
-      v[r] = make_float2(row(gx), row(gx + 1));
+      const int lx = 2 * (j + r * NR);
+      const int gx = ox + lx;
+      float a = row(gx), b = row(gx + 1);
+      if (MASK) {
+        a = (yin && lx >= x0 && lx < x1) ? a : 0.f;
+        b = (yin && lx + 1 >= x0 && lx + 1 < x1) ? b : 0.f;
+      }
+      v[r] = make_float2(a, b);
     }
   }
 };
@@ -399,7 +471,9 @@ __device__ __forceinline__ void run_transform_to(const FftPlan* __restrict__ p, 
 // ------------------------------------------------------------------------------------------
 // kernels (templated on gather / epilogue; instantiated in passes_*.cu)
 // ------------------------------------------------------------------------------------------
-template <class Gather>
+// MASK: the gathered values are kept only inside the tile's effective region (tiles then
+// partition the volume; used for the PSF gradient's correlation).
+template <class Gather, bool MASK = false>
 __global__ void __launch_bounds__(kThreads, 2)
 plane_fwd_kernel(const TileDesc* __restrict__ tiles, const int2* __restrict__ items,
                  const FftPlan* __restrict__ plans, float2* __restrict__ spec, Gather gather) {
@@ -411,7 +485,8 @@ plane_fwd_kernel(const TileDesc* __restrict__ tiles, const int2* __restrict__ it
   float2* cur = sm;
   float2* oth = sm + t.ty * t.pitch;
   // x: R2C of every row (packed pairs gathered straight from the volume)
-  RowGather<Gather> ld0{gather, t.ox, t.oy, t.oz + z};
+  RowGather<Gather, MASK> ld0{gather, t.ox, t.oy, t.oz + z, t.hx, t.hx + t.ex, t.hy, t.hy + t.ey,
+                              z >= t.hz && z < t.hz + t.ez};
   const FftPlan* pxp = plans + t.plan_x;
   run_transform_smem<false, true>(pxp, t.ty, ld0, cur, oth, 1, t.pitch);
   r2c_post(cur, t.ty, M, t.pitch, pxp->tw_r2c);
@@ -448,7 +523,8 @@ plane_inv_kernel(const TileDesc* __restrict__ tiles, const int2* __restrict__ it
   epi.finish();
 }
 
-// MODE 0: forward z, multiply by the OTF, inverse z.  MODE 1: forward z and scale (OTF build).
+// MODE 0: forward z, multiply by the OTF, inverse z.  MODE 1: forward z and scale (OTF build,
+// spectra of the PSF gradient).  MODE 2: inverse z only.
 // OCC: CTAs per SM the register allocation is sized for.
 template <int MODE, int OCC = 2>
 __global__ void __launch_bounds__(kZThreads, OCC)
@@ -470,6 +546,10 @@ zpass_kernel(const TileDesc* __restrict__ tiles, const int2* __restrict__ items,
   const float2* tw = pz->tw;
   if (MODE == 1) {
     run_transform_to<false, false>(pz, count, g, PencilScaledStore{g.p, plane, scale}, cur, oth, kZPitch, 1);
+    return;
+  }
+  if (MODE == 2) {  // inverse only
+    run_transform_to<true, false>(pz, count, g, g, cur, oth, kZPitch, 1);
     return;
   }
   OtfMul mul{otf + t.otf_off + p0, plane};

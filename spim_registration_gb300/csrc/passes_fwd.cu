@@ -3,11 +3,11 @@
 
 namespace mvd {
 
-template <class Gather>
+template <class Gather, bool MASK = false>
 static void launch_fwd_impl(PlanTable& pt, const TileDesc* tiles, const int2* items, int nitems, size_t smem,
                             float2* spec, Gather g, cudaStream_t s) {
   if (nitems == 0) return;
-  auto k = plane_fwd_kernel<Gather>;
+  auto k = plane_fwd_kernel<Gather, MASK>;
   set_smem(k, smem);
   k<<<nitems, kThreads, smem, s>>>(tiles, items, pt.device(), spec, g);
   MVD_CHECK(cudaGetLastError());
@@ -31,6 +31,12 @@ void launch_fwd_value_items(PlanTable& pt, const ConvPlan& p, const TileDesc* ti
                             const float* vol, int vx, int vy, int vz, float value, float2* spec, cudaStream_t s) {
   GatherValue g{{vol, vx, vy, vz}, value};
   launch_fwd_impl(pt, tiles, items, nitems, p.smem_plane, spec, g, s);
+}
+
+void launch_fwd_masked(PlanTable& pt, const ConvPlan& p, const float* vol, float2* spec, cudaStream_t s) {
+  GatherValue g{{vol, p.nx, p.ny, p.nz}, 0.f};
+  launch_fwd_impl<GatherValue, true>(pt, p.d_tiles.as<TileDesc>(), p.d_items_fwd.as<int2>(), (int)p.items_fwd.size(),
+                                     p.smem_plane, spec, g, s);
 }
 
 }  // namespace mvd

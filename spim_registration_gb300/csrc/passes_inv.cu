@@ -31,4 +31,20 @@ void launch_inv_update(PlanTable& pt, const ConvPlan& p, const float2* spec, flo
   launch_inv_impl(pt, p, spec, e, s);
 }
 
+void launch_inv_nll(PlanTable& pt, const ConvPlan& p, const float2* spec, const float* img, const float* w, float* r,
+                    double* nll, cudaStream_t s) {
+  EpiNll e{img, w, r, nll, p.nx, p.ny, 0.f};
+  launch_inv_impl(pt, p, spec, e, s);
+}
+
+void launch_inv_store_items(PlanTable& pt, const ConvPlan& p, const TileDesc* tiles, const int2* items, int nitems,
+                            const float2* spec, float* out, int nx, int ny, cudaStream_t s) {
+  if (nitems == 0) return;
+  auto k = plane_inv_kernel<EpiStore>;
+  set_smem(k, p.smem_plane);
+  k<<<nitems, kThreads, p.smem_plane, s>>>(tiles, items, pt.device(), spec, EpiStore{out, nx, ny});
+  MVD_CHECK(cudaGetLastError());
+  count_launch();
+}
+
 }  // namespace mvd

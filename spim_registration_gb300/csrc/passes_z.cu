@@ -35,4 +35,18 @@ void launch_z_forward_scaled(PlanTable& pt, const ConvPlan& p, const TileDesc* t
   count_launch();
 }
 
+void launch_z_forward(PlanTable& pt, const ConvPlan& p, float2* spec, cudaStream_t s) {
+  launch_z_forward_scaled(pt, p, p.d_tiles.as<TileDesc>(), p.d_items_z.as<int2>(), (int)p.items_z.size(), spec, 1.f, s);
+}
+
+void launch_z_inverse_items(PlanTable& pt, const ConvPlan& p, const TileDesc* tiles, const int2* items, int nitems,
+                            float2* spec, cudaStream_t s) {
+  if (nitems == 0) return;
+  auto k = zpass_kernel<2>;
+  set_smem(k, p.smem_z);
+  k<<<nitems, kZThreads, p.smem_z, s>>>(tiles, items, pt.device(), spec, nullptr, 1.f);
+  MVD_CHECK(cudaGetLastError());
+  count_launch();
+}
+
 }  // namespace mvd

@@ -230,6 +230,26 @@ class Deconvolution:
         names = ["plane_fwd", "zpass", "plane_inv_quotient", "plane_inv_update", "other"]
         return {n: (ms[i], ln[i]) for i, n in enumerate(names)}
 
+    def forward(self) -> float:
+        """Poisson NLL of the image-formation model at the current psi and kernel1 (FP64)."""
+        d = ctypes.c_double()
+        native.check(self.lib.mvd_forward(self.h, ctypes.byref(d)))
+        return d.value
+
+    def backward(self):
+        """(dNLL/dpsi, [dNLL/dkernel1_v]) at the current psi and kernel1."""
+        g = np.empty(self.shape, dtype=np.float32)
+        gk = [np.empty(s, dtype=np.float32) for s in self.psf_shapes]
+        ptrs = (native._F * self.n_views)(*[native.fptr(a) for a in gk])
+        native.check(self.lib.mvd_backward(self.h, native.fptr(g), ptrs))
+        return g, gk
+
+    def set_kernel(self, view: int, which: int, data: np.ndarray):
+        data = np.ascontiguousarray(data, dtype=np.float32)
+        if data.shape != self.psf_shapes[view]:
+            raise ValueError("kernel has the wrong shape")
+        native.check(self.lib.mvd_set_kernel(self.h, view, which, native.fptr(data)))
+
     def plan(self, view: int):
         t, s, e = (ctypes.c_int * 3)(), (ctypes.c_int * 3)(), (ctypes.c_int * 3)()
         pv = ctypes.c_longlong()

@@ -70,6 +70,9 @@ SIGNATURES = {
     "mvd_get_stream": (ctypes.c_int, [_H, ctypes.POINTER(ctypes.c_void_p)]),
     "mvd_get_launch_count": (ctypes.c_int, [_H, _LL]),
     "mvd_profile_iteration": (ctypes.c_int, [_H, _D, _I]),
+    "mvd_forward": (ctypes.c_int, [_H, _D]),
+    "mvd_backward": (ctypes.c_int, [_H, _F, ctypes.POINTER(_F)]),
+    "mvd_set_kernel": (ctypes.c_int, [_H, ctypes.c_int, ctypes.c_int, _F]),
 }
 
 

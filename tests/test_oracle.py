@@ -159,3 +159,27 @@ def test_blocked_deconvolution_equals_whole():
     a, _ = O.deconvolve(p, block=None)
     b, _ = O.deconvolve(p, block=(24, 20, 20))
     np.testing.assert_allclose(a, b, rtol=1e-10, atol=1e-10)
+
+
+def test_nll_gradient_matches_central_differences():
+    p = S.make_problem(5, shape_xyz=(14, 12, 10), psf_size_xyz=(3, 3, 5), n_blobs=6, n_views=2)
+    psi = p.views[0].astype(np.float64) * 0.9 + 3
+    psfs = [q.astype(np.float64) for q in p.psfs]
+    gp, gk = O.poisson_nll_grad(psi, p.views, p.weights, psfs)
+    r = rng(9)
+    for _ in range(6):
+        i = tuple(int(r.integers(0, s)) for s in psi.shape)
+        a, b = psi.copy(), psi.copy()
+        a[i] += 1e-4
+        b[i] -= 1e-4
+        fd = (O.poisson_nll(a, p.views, p.weights, psfs) - O.poisson_nll(b, p.views, p.weights, psfs)) / 2e-4
+        assert gp[i] == pytest.approx(fd, rel=1e-4, abs=1e-6)
+    for t in range(6):
+        v = t % 2
+        i = tuple(int(r.integers(0, s)) for s in psfs[v].shape)
+        a = [q.copy() for q in psfs]
+        b = [q.copy() for q in psfs]
+        a[v][i] += 1e-5
+        b[v][i] -= 1e-5
+        fd = (O.poisson_nll(psi, p.views, p.weights, a) - O.poisson_nll(psi, p.views, p.weights, b)) / 2e-5
+        assert gk[v][i] == pytest.approx(fd, rel=1e-4)
