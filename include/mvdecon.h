@@ -66,7 +66,8 @@ enum {
 enum {
   MVD_FLAG_PLAIN = 1,    /* reference structure: one block per launch sequence, separate
                             quotient / update kernels, no graph (the plain FP32 GPU form) */
-  MVD_FLAG_NO_GRAPH = 2  /* batched, fused passes but launched eagerly (no CUDA graph) */
+  MVD_FLAG_NO_GRAPH = 2, /* batched, fused passes but launched eagerly (no CUDA graph) */
+  MVD_FLAG_AUTOTUNE = 4  /* time candidate tile plans per view at creation and keep the fastest */
 };
 
 /* Last error message of the calling thread ("" if none). */
@@ -103,8 +104,10 @@ int mvd_convolve3d_device_noalloc(const float* in, float* out, const int* dims_x
  * (spim/process/fusion/deconvolution/MVDeconvolution.java:94-211, MVDeconFFT.java:79-324)
  * mvd_create uploads the views, weights and PSFs, prepares kernel1/kernel2 per PSFTYPE
  * (MVDeconFFT.init), their spectra and the tile plans, and initialises psi with the average
- * of the first iteration (MVDeconvolution.java:133-147).  block_xyz selects the reference's
- * block size for MVD_FLAG_PLAIN (NULL = one block of image + kernel - 1). */
+ * of the first iteration (MVDeconvolution.java:133-147).  Each view's convolutions cover only
+ * the bounding box of its data (img > 0 or weight > 0), with all of its tiles, of whatever
+ * shape, in one launch per pass.  block_xyz selects the reference's block size for
+ * MVD_FLAG_PLAIN (NULL = one block of image + kernel - 1). */
 typedef struct mvd_decon mvd_decon;
 
 int mvd_create(mvd_decon** out, int devCUDA, const int* dims_xyz, int num_views,

@@ -5,6 +5,7 @@ The compute path is ``lib/libFourierConvolutionCUDA.so`` (sm_103a CUDA, C ABI in
 Python mirror of the reference's Java classes.
 """
 from .mvdecon import (  # noqa: F401
+    FLAG_AUTOTUNE,
     FLAG_NO_GRAPH,
     FLAG_PLAIN,
     PSFTYPE,

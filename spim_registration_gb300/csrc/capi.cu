@@ -1,6 +1,7 @@
 // C ABI of libFourierConvolutionCUDA: the reference's JNA entry points and the
 // whole-deconvolution handle.  Every entry point catches exceptions and turns them into a
 // status code plus a per-thread message; nothing is retained across calls except in handles.
+#include <algorithm>
 #include <array>
 #include <cstdio>
 #include <map>
@@ -517,6 +518,96 @@ void prepare_kernels(mvd_decon* h) {
   }
 }
 
+// Bounding box of the voxels where a view has data (img > 0) or weight (w > 0).  Outside it
+// the quotient is 1 (MVDeconvolution.java:519-522) and the update leaves psi unchanged
+// (weight 0, :723), so a view's convolutions only need to cover this box.  An empty box
+// falls back to the whole volume.
+void data_box(const float* img, const float* w, const int* dims, int lo[3], int hi[3]) {
+  const int nx = dims[0], ny = dims[1], nz = dims[2];
+  int l[3] = {nx, ny, nz}, u[3] = {-1, -1, -1};
+  for (int z = 0; z < nz; ++z)
+    for (int y = 0; y < ny; ++y) {
+      const size_t row = ((size_t)z * ny + y) * nx;
+      int first = -1, last = -1;
+      for (int x = 0; x < nx; ++x)
+        if (img[row + x] > 0.f || w[row + x] > 0.f) {
+          if (first < 0) first = x;
+          last = x;
+        }
+      if (first < 0) continue;
+      l[0] = std::min(l[0], first);
+      u[0] = std::max(u[0], last);
+      l[1] = std::min(l[1], y);
+      u[1] = std::max(u[1], y);
+      l[2] = std::min(l[2], z);
+      u[2] = std::max(u[2], z);
+    }
+  for (int d = 0; d < 3; ++d) {
+    if (u[d] < 0) {  // no data at all
+      for (int e = 0; e < 3; ++e) {
+        lo[e] = 0;
+        hi[e] = dims[e];
+      }
+      return;
+    }
+    lo[d] = l[d];
+    hi[d] = u[d] + 1;
+  }
+}
+
+// Tile plan of a view over its data box; with `autotune` the plane budgets below are all
+// tried and the fastest plan (one timed view stage each) is kept.
+std::unique_ptr<ConvPlan> plan_view(mvd_decon* h, int v, const int lo[3], const int hi[3], bool autotune) {
+  const auto& k = h->kd[v];
+  const int n[3] = {hi[0] - lo[0], hi[1] - lo[1], hi[2] - lo[2]};
+  const bool full = lo[0] == 0 && lo[1] == 0 && lo[2] == 0 && hi[0] == h->dims[0] && hi[1] == h->dims[1] &&
+                    hi[2] == h->dims[2];
+  auto make = [&](int cap) {
+    PlanOptions o;
+    o.cap = cap;
+    auto p = make_conv_plan(h->pt, n[0], n[1], n[2], k[0], k[1], k[2], o);
+    if (!full) place_plan(*p, lo[0], lo[1], lo[2], h->dims);
+    return p;
+  };
+  if (!autotune) return make(0);
+  std::unique_ptr<ConvPlan> best;
+  float best_ms = 1e30f;
+  std::vector<std::array<int, 3>> seen;
+  for (int cap : {4608, 7168, 10240, 14336}) {
+    auto p = make(cap);
+    const std::array<int, 3> shape{p->ax.T, p->ay.T, p->az.T};
+    if (std::find(seen.begin(), seen.end(), shape) != seen.end()) continue;
+    seen.push_back(shape);
+    DevBuf otf(p->otf_elems * sizeof(float2)), spec(p->spec_elems * sizeof(float2));
+    MVD_CHECK(cudaMemsetAsync(otf.p, 0, otf.bytes, h->stream));
+    cudaEvent_t e0, e1;
+    MVD_CHECK(cudaEventCreate(&e0));
+    MVD_CHECK(cudaEventCreate(&e1));
+    float ms = 1e30f;
+    for (int rep = 0; rep < 4; ++rep) {  // rep 0 warms up
+      MVD_CHECK(cudaEventRecord(e0, h->stream));
+      launch_fwd_mirror(h->pt, *p, h->psi.as<float>(), spec.as<float2>(), h->stream);
+      launch_z(h->pt, *p, spec.as<float2>(), otf.as<float2>(), h->stream);
+      launch_inv_quotient(h->pt, *p, spec.as<float2>(), h->img[v].as<float>(), h->q.as<float>(), h->stream);
+      launch_fwd_value(h->pt, *p, h->q.as<float>(), 1.f, spec.as<float2>(), h->stream);
+      launch_z(h->pt, *p, spec.as<float2>(), otf.as<float2>(), h->stream);
+      launch_inv_quotient(h->pt, *p, spec.as<float2>(), h->img[v].as<float>(), h->q.as<float>(), h->stream);
+      MVD_CHECK(cudaEventRecord(e1, h->stream));
+      MVD_CHECK(cudaEventSynchronize(e1));
+      float t = 0.f;
+      MVD_CHECK(cudaEventElapsedTime(&t, e0, e1));
+      if (rep > 0) ms = std::min(ms, t);
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (ms < best_ms) {
+      best_ms = ms;
+      best = std::move(p);
+    }
+  }
+  return best;
+}
+
 std::unique_ptr<ConvPlan> block_plan(PlanTable& pt, const std::array<int, 3>& b, const std::array<int, 3>& k) {
   // the block convolved as a volume (mirror-single at its own border); its interior is what
   // the paste consumes
@@ -577,6 +668,8 @@ extern "C" int mvd_create(mvd_decon** out, int devCUDA, const int* dims, int num
   prepare_kernels(h.get());
   h->psi.alloc(nb);
   h->q.alloc(nb);
+  MVD_CHECK(cudaMemsetAsync(h->psi.p, 0, nb, h->stream));
+  MVD_CHECK(cudaMemsetAsync(h->q.p, 0, nb, h->stream));
   long long spec_max = 0;
   if (flags & MVD_FLAG_PLAIN) {
     h->tmp2.alloc(nb);
@@ -592,8 +685,11 @@ extern "C" int mvd_create(mvd_decon** out, int devCUDA, const int* dims, int num
     h->blk_in.alloc(blk_max * sizeof(float));
     h->blk_out.alloc(blk_max * sizeof(float));
   } else {
-    for (int v = 0; v < num_views; ++v)
-      h->plans.push_back(make_conv_plan(h->pt, dims[0], dims[1], dims[2], h->kd[v][0], h->kd[v][1], h->kd[v][2]));
+    for (int v = 0; v < num_views; ++v) {
+      int lo[3], hi[3];
+      data_box(views[v], weights[v], dims, lo, hi);
+      h->plans.push_back(plan_view(h.get(), v, lo, hi, (flags & MVD_FLAG_AUTOTUNE) != 0));
+    }
   }
   for (int v = 0; v < num_views; ++v) {
     const ConvPlan& p = *h->plans[v];
@@ -960,6 +1056,7 @@ extern "C" int mvd_backward(mvd_decon* h, float* grad_psi, float* const* grad_ps
   cudaStream_t s = h->stream;
   MVD_CHECK(cudaMemsetAsync(h->g_psi.p, 0, h->N * sizeof(float), s));
   MVD_CHECK(cudaMemsetAsync(h->d_nll.p, 0, sizeof(double), s));
+  MVD_CHECK(cudaMemsetAsync(h->r.p, 0, h->N * sizeof(float), s));  // zero outside the views' data boxes
   for (int v = 0; v < h->V; ++v) {
     const ConvPlan& p = *h->plans[v];
     mvd_decon::AdjView& a = h->adj[v];

@@ -224,7 +224,7 @@ std::unique_ptr<ConvPlan> make_conv_plan(PlanTable& pt, int nx, int ny, int nz, 
   AxisTiles bx, by, bz;
   for (auto& a : ox)
     for (auto& b : oy) {
-      if ((long long)row_pitch(a.T / 2) * b.T > plane_cap()) continue;
+      if ((long long)row_pitch(a.T / 2) * b.T > (opt.cap > 0 ? opt.cap : plane_cap())) continue;
       for (auto& c : oz) {
         const double ntiles = (double)a.n * b.n * c.n;
         const double cost = ntiles * a.T * b.T * c.T * (1.0 + 1e-3 * ntiles);
@@ -241,6 +241,8 @@ std::unique_ptr<ConvPlan> make_conv_plan(PlanTable& pt, int nx, int ny, int nz, 
   ConvPlan& p = *plan;
   p.nx = nx; p.ny = ny; p.nz = nz;
   p.kx = kx; p.ky = ky; p.kz = kz;
+  p.vol[0] = nx; p.vol[1] = ny; p.vol[2] = nz;
+  p.box_hi[0] = nx; p.box_hi[1] = ny; p.box_hi[2] = nz;
   p.ax = bx; p.ay = by; p.az = bz;
   const int px = bx.T / 2 + 1;
   const int pitch = row_pitch(bx.T / 2);
@@ -273,6 +275,21 @@ std::unique_ptr<ConvPlan> make_conv_plan(PlanTable& pt, int nx, int ny, int nz, 
   fill_items(p);
   p.upload();
   return plan;
+}
+
+void place_plan(ConvPlan& p, int dx, int dy, int dz, const int vol[3]) {
+  for (auto& t : p.tiles) {
+    t.ox += dx;
+    t.oy += dy;
+    t.oz += dz;
+  }
+  const int d[3] = {dx, dy, dz}, n[3] = {p.nx, p.ny, p.nz};
+  for (int i = 0; i < 3; ++i) {
+    p.vol[i] = vol[i];
+    p.box_lo[i] = d[i];
+    p.box_hi[i] = d[i] + n[i];
+  }
+  p.upload();
 }
 
 std::string describe(const ConvPlan& p) {

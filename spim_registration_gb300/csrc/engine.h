@@ -66,8 +66,12 @@ struct AxisTiles {
 // A convolution plan over one volume with one kernel size: the tiles, their work items and
 // the spectrum / OTF layout.
 struct ConvPlan {
-  int nx = 0, ny = 0, nz = 0;          // volume
+  int nx = 0, ny = 0, nz = 0;          // region the tiles cover (their effective regions)
   int kx = 0, ky = 0, kz = 0;          // kernel
+  // the volume the gathers and epilogues address (tile coordinates are in its frame), and the
+  // data box of a value-extended input (value outside it); by default the covered region
+  int vol[3] = {0, 0, 0};
+  int box_lo[3] = {0, 0, 0}, box_hi[3] = {0, 0, 0};
   AxisTiles ax, ay, az;
   std::vector<TileDesc> tiles;         // host copy
   std::vector<int2> items_fwd, items_inv, items_z;
@@ -81,7 +85,12 @@ struct ConvPlan {
 
 struct PlanOptions {
   int force_tx = 0, force_ty = 0, force_tz = 0;  // 0 = planner's choice
+  int cap = 0;                                   // plane-buffer budget; 0 = plane_cap()
 };
+
+// Move a plan's tiles by (dx, dy, dz) into the frame of a larger volume `vol` whose data box
+// is the covered region (the tiles then cover [d, d + n) of that volume); re-uploads the tiles.
+void place_plan(ConvPlan& p, int dx, int dy, int dz, const int vol[3]);
 
 // Choose tiles for a (volume, kernel) pair; effective regions cover the whole volume.
 std::unique_ptr<ConvPlan> make_conv_plan(PlanTable& pt, int nx, int ny, int nz, int kx, int ky,

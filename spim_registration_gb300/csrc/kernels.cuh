@@ -85,17 +85,30 @@ struct GatherMirror {  // psi extended mirror-single (MVDeconFFTThreads.java:44,
 struct GatherValue {  // quotient extended with a constant (value 1: MVDeconFFTThreads.java:63,103)
   VolumeRef v;
   float value;
+  int lo[3], hi[3];  // the data box (x, y, z): `value` outside it
+  __host__ __device__ static GatherValue full(const float* data, int nx, int ny, int nz, float value) {
+    return box(data, nx, ny, nz, value, 0, 0, 0, nx, ny, nz);
+  }
+  __host__ __device__ static GatherValue box(const float* data, int nx, int ny, int nz, float value, int x0, int y0,
+                                             int z0, int x1, int y1, int z1) {
+    GatherValue g;
+    g.v = VolumeRef{data, nx, ny, nz};
+    g.value = value;
+    g.lo[0] = x0; g.lo[1] = y0; g.lo[2] = z0;
+    g.hi[0] = x1; g.hi[1] = y1; g.hi[2] = z1;
+    return g;
+  }
   struct Row {
-    const float* p;  // nullptr: the whole row is outside the volume
-    int nx;
+    const float* p;  // nullptr: the whole row is outside the box
+    int x0, x1;
     float value;
     __device__ __forceinline__ float operator()(int gx) const {
-      return (p && gx >= 0 && gx < nx) ? __ldg(p + gx) : value;
+      return (p && gx >= x0 && gx < x1) ? __ldg(p + gx) : value;
     }
   };
   __device__ __forceinline__ Row row(int gy, int gz) const {
-    const bool in = gy >= 0 && gz >= 0 && gy < v.ny && gz < v.nz;
-    return Row{in ? v.data + ((long long)gz * v.ny + gy) * v.nx : nullptr, v.nx, value};
+    const bool in = gy >= lo[1] && gz >= lo[2] && gy < hi[1] && gz < hi[2];
+    return Row{in ? v.data + ((long long)gz * v.ny + gy) * v.nx : nullptr, lo[0], hi[0], value};
   }
   __device__ __forceinline__ float operator()(int gx, int gy, int gz) const { return row(gy, gz)(gx); }
 };

@@ -270,7 +270,7 @@ extern "C" int mvd_convolve3d_device_noalloc(const float* in, float* out, const 
     smem_attr(plane_fwd_kernel<GatherValue>, smem_plane);
     plane_fwd_kernel<GatherValue><<<(int)otf_fwd.size(), kThreads, smem_plane, s>>>(
         d_tiles, reinterpret_cast<const int2*>(base + o_ofwd), d_plans, d_otf,
-        GatherValue{{d_place, bx.T, by.T, bz.T}, 0.f});
+        GatherValue::full(d_place, bx.T, by.T, bz.T, 0.f));
     MVD_CHECK(cudaGetLastError());
     smem_attr(zpass_kernel<1>, smem_z);
     zpass_kernel<1><<<(int)otf_z.size(), kZThreads, smem_z, s>>>(d_tiles, reinterpret_cast<const int2*>(base + o_oz),
@@ -286,7 +286,7 @@ extern "C" int mvd_convolve3d_device_noalloc(const float* in, float* out, const 
           d_tiles, d_fwd, d_plans, d_spec, GatherMirror{{in, nx, ny, nz}});
     } else {
       plane_fwd_kernel<GatherValue><<<(int)fwd.size(), kThreads, smem_plane, s>>>(
-          d_tiles, d_fwd, d_plans, d_spec, GatherValue{{in, nx, ny, nz}, ext_value});
+          d_tiles, d_fwd, d_plans, d_spec, GatherValue::full(in, nx, ny, nz, ext_value));
     }
     MVD_CHECK(cudaGetLastError());
     smem_attr(zpass_kernel<0>, smem_z);

@@ -15,25 +15,25 @@ static void launch_inv_impl(PlanTable& pt, const ConvPlan& p, const float2* spec
 }
 
 void launch_inv_store(PlanTable& pt, const ConvPlan& p, const float2* spec, float* out, cudaStream_t s) {
-  EpiStore e{out, p.nx, p.ny};
+  EpiStore e{out, p.vol[0], p.vol[1]};
   launch_inv_impl(pt, p, spec, e, s);
 }
 
 void launch_inv_quotient(PlanTable& pt, const ConvPlan& p, const float2* spec, const float* img, float* q,
                          cudaStream_t s) {
-  EpiQuotient e{img, q, p.nx, p.ny};
+  EpiQuotient e{img, q, p.vol[0], p.vol[1]};
   launch_inv_impl(pt, p, spec, e, s);
 }
 
 void launch_inv_update(PlanTable& pt, const ConvPlan& p, const float2* spec, float* psi, const float* weight,
                        float lambda, double* stat_sum, unsigned* stat_max, cudaStream_t s) {
-  EpiUpdate e{psi, weight, lambda, stat_sum, stat_max, p.nx, p.ny, 0.f, 0.f};
+  EpiUpdate e{psi, weight, lambda, stat_sum, stat_max, p.vol[0], p.vol[1], 0.f, 0.f};
   launch_inv_impl(pt, p, spec, e, s);
 }
 
 void launch_inv_nll(PlanTable& pt, const ConvPlan& p, const float2* spec, const float* img, const float* w, float* r,
                     double* nll, cudaStream_t s) {
-  EpiNll e{img, w, r, nll, p.nx, p.ny, 0.f};
+  EpiNll e{img, w, r, nll, p.vol[0], p.vol[1], 0.f};
   launch_inv_impl(pt, p, spec, e, s);
 }
 

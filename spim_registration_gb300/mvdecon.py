@@ -34,6 +34,7 @@ class PSFTYPE(enum.IntEnum):
 
 FLAG_PLAIN = 1
 FLAG_NO_GRAPH = 2
+FLAG_AUTOTUNE = 4
 
 
 class CUDAFourierConvolution:

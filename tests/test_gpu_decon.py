@@ -129,3 +129,26 @@ def test_single_view_and_invalid_arguments():
         Deconvolution(p.views, p.weights, [np.ones((4, 3, 3), np.float32)], p.psftype, p.lam)
     with pytest.raises(MvdError):
         Deconvolution(p.views, p.weights, p.psfs, 7, p.lam)
+
+
+def test_cropped_views_are_tiled_over_their_data_box_only():
+    p = small(3, S.EFFICIENT_BAYESIAN, it=2)
+    d = Deconvolution(p.views, p.weights, p.psfs, p.psftype, p.lam)
+    full = Deconvolution([np.maximum(v, 1.0).astype(np.float32) for v in p.views],
+                         [np.ones_like(w) for w in p.weights], p.psfs, p.psftype, p.lam)
+    cropped = sum(d.plan(v)["padded_voxels"] for v in range(len(p.views)))
+    whole = sum(full.plan(v)["padded_voxels"] for v in range(len(p.views)))
+    assert cropped < 0.8 * whole
+    # the result is the reference's on the whole volume
+    ref, _ = O.deconvolve(p, arith="f64", block=None, mask=False)
+    d.run(p.iterations)
+    assert rel_l2(d.get_psi(), ref) < RELL2
+
+
+def test_autotuned_plans_give_the_same_result():
+    from spim_registration_gb300 import FLAG_AUTOTUNE
+
+    p = small(2, S.EFFICIENT_BAYESIAN, it=3)
+    a = run_gpu(p).get_psi()
+    b = run_gpu(p, FLAG_AUTOTUNE).get_psi()
+    assert rel_l2(b, a) < 1e-5
