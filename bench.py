@@ -36,6 +36,7 @@ METRIC = "voxel-updates/s, 4-view decon, batched+split vs plain FP32 form at rel
 WORKLOADS = {
     # name: (cfg id, shape xyz, psf xyz, reference block for the plain form)
     "cfg2_4view_eb_256x256x192": (2, (256, 256, 192), (15, 15, 41), (128, 128, 128)),
+    "cfg3_6view_crops_256": (3, (256, 256, 256), (15, 15, 41), (128, 128, 128)),
     "cfg4_4view_eb_512x512x256": (4, (512, 512, 256), (31, 31, 61), None),
     "cfg1_2view_128x128x64": (1, (128, 128, 64), (9, 9, 25), None),
 }
@@ -52,6 +53,7 @@ def parse():
     ap.add_argument("--no-plain", action="store_true", help="skip the plain FP32 form measurement")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true", help="planner's default tiles instead of timed ones")
     return ap.parse_args()
 
 
@@ -182,7 +184,7 @@ def replica_value(units_per_rank: float, ms_max: float, world: int) -> float:
 def run_ours(args, rank, world, local):
     import torch
 
-    from spim_registration_gb300 import FLAG_PLAIN, Deconvolution
+    from spim_registration_gb300 import FLAG_AUTOTUNE, FLAG_PLAIN, Deconvolution
     from spim_registration_gb300 import native
 
     torch.cuda.set_device(local)
@@ -199,7 +201,8 @@ def run_ours(args, rank, world, local):
     V = len(prob.views)
     lib = native.load()
 
-    dec = Deconvolution(prob.views, prob.weights, prob.psfs, prob.psftype, prob.lam, local, 0)
+    dec = Deconvolution(prob.views, prob.weights, prob.psfs, prob.psftype, prob.lam, local,
+                        0 if args.no_autotune else FLAG_AUTOTUNE)
     stream = torch.cuda.ExternalStream(dec.stream(), device=local)
 
     # warm-up (captures the graph on the first iteration)
@@ -262,7 +265,7 @@ def run_ours(args, rank, world, local):
         "config": {"workload": args.workload, "views": V, "volume_xyz": list(prob.dims_xyz),
                    "psf_xyz": [list(p.shape[::-1]) for p in prob.psfs], "psftype": "EFFICIENT_BAYESIAN",
                    "lambda": prob.lam, "step": "one iteration over all views",
-                   "plans": [dec.plan(v) for v in range(V)],
+                   "plans": [dec.plan(v) for v in range(V)], "flags": "planner default tiles" if args.no_autotune else "autotuned tile plans",
                    "l2": "working set per iteration > 129 MB L2 (no flush needed)",
                    "parallelism": f"replicas x{world}"},
         "gpu_launches": launches,

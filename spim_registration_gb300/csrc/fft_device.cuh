@@ -358,77 +358,4 @@ struct Smem {
   }
 };
 
-// ---------------------------------------------------------------------------------------
-// Real <-> half-complex post/pre-processing of rows.  A row of 2M reals packed as M complex
-// values z[n] = x[2n] + i x[2n+1] was transformed to Z = FFT_M(z); the post-step turns it
-// into X[k], k = 0..M, of the length-2M real transform, writing X[M] to slot M.
-// The pre-step is its inverse up to a factor 2 (together with an unnormalised inverse
-// FFT_M it yields 2M * x).  `tw2` = exp(-2 pi i k / (2M)), k in [0, M].
-// Rows are d + r * pitch for r in [0, rows); no barrier inside.
-// ---------------------------------------------------------------------------------------
-__device__ __forceinline__ void r2c_post(float2* d, int rows, int M, int pitch, const float2* __restrict__ tw2) {
-  const int half = M / 2;  // pairs (k, M-k) for k = 0..half
-  const int total = rows * (half + 1);
-  for (int i = threadIdx.x; i < total; i += blockDim.x) {
-    const int row = i % rows;
-    const int k = i / rows;
-    float2* r = d + row * pitch;
-    if (k == 0) {
-      float2 z0 = r[0];
-      r[0] = make_float2(z0.x + z0.y, 0.f);
-      r[M] = make_float2(z0.x - z0.y, 0.f);
-      continue;
-    }
-    const int k2 = M - k;
-    float2 zk = r[k], zc = r[k2];
-    // X[k] = e - i w^k o,  e = (Zk + conj Zc)/2,  o = (Zk - conj Zc)/2
-    float2 e = make_float2(0.5f * (zk.x + zc.x), 0.5f * (zk.y - zc.y));
-    float2 o = make_float2(0.5f * (zk.x - zc.x), 0.5f * (zk.y + zc.y));
-    float2 w = __ldg(tw2 + k);
-    float2 wo = cmul(w, o);
-    float2 xk = make_float2(e.x + wo.y, e.y - wo.x);
-    if (k2 == k) {
-      r[k] = xk;
-    } else {
-      // X[M-k] = conj(e) - i conj(w^k o)   (uses w^{M-k} = -conj(w^k))
-      r[k] = xk;
-      r[k2] = make_float2(e.x - wo.y, -e.y - wo.x);
-    }
-  }
-}
-
-__device__ __forceinline__ void c2r_pre(float2* d, int rows, int M, int pitch, const float2* __restrict__ tw2) {
-  const int half = M / 2;
-  const int total = rows * (half + 1);
-  for (int i = threadIdx.x; i < total; i += blockDim.x) {
-    const int row = i % rows;
-    const int k = i / rows;
-    float2* r = d + row * pitch;
-    if (k == 0) {
-      float2 x0 = r[0], xm = r[M];
-      // Z[0] = (X0 + conj XM) + i (X0 - conj XM)
-      float2 e = make_float2(x0.x + xm.x, x0.y - xm.y);
-      float2 o = make_float2(x0.x - xm.x, x0.y + xm.y);
-      r[0] = make_float2(e.x - o.y, e.y + o.x);
-      continue;
-    }
-    const int k2 = M - k;
-    float2 xk = r[k], xc = r[k2];
-    // Z[k] = (Xk + conj Xc) + i conj(w^k) (Xk - conj Xc)
-    float2 e = make_float2(xk.x + xc.x, xk.y - xc.y);
-    float2 o = make_float2(xk.x - xc.x, xk.y + xc.y);
-    float2 w = __ldg(tw2 + k);
-    float2 wo = cmul(cconj(w), o);
-    float2 zk = make_float2(e.x - wo.y, e.y + wo.x);
-    if (k2 == k) {
-      r[k] = zk;
-    } else {
-      // Z[M-k] = conj(e) + i w^k conj(o)   (uses conj(w^{M-k}) = -w^k)
-      float2 wo2 = cmul(w, cconj(o));
-      r[k] = zk;
-      r[k2] = make_float2(e.x - wo2.y, -e.y + wo2.x);
-    }
-  }
-}
-
 }  // namespace mvd

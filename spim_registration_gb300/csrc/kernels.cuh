@@ -10,18 +10,21 @@
 //
 // Three passes per convolution, all driven by work-item tables so that every tile of every
 // shape runs in the same launch:
-//   plane_fwd : gather a z-slice of the tile (with the out-of-bounds rule), R2C along x,
-//               C2C along y, store the half-spectrum slice  [z][y][kx] (kx fastest);
+//   plane_fwd : gather a z-slice of the tile (with the out-of-bounds rule), R2C along x (a
+//               half-length complex FFT of packed pairs; the real-spectrum step is folded
+//               into the first y stage's loads), C2C along y, store the half-spectrum slice
+//               [z][y][kx] (kx fastest);
 //   zpass     : for 32 consecutive (y, kx) pencils: C2C along z, multiply by the OTF,
 //               inverse C2C along z (or, for OTF preparation, forward only and scale);
-//   plane_inv : for an effective z-slice: inverse C2C along y, C2R along x, epilogue over
-//               the effective (x, y) region (store / quotient / multiplicative update).
+//   plane_inv : for an effective z-slice: inverse C2C along y, C2R along x of the effective
+//               rows only (the half-spectrum step folded into the first x stage's loads),
+//               epilogue over the effective (x, y) region (store / quotient / update / NLL).
 #pragma once
 #include "fft_device.cuh"
 
 namespace mvd {
 
-constexpr int kThreads = 256;    // threads per CTA of the plane kernels (two CTAs fit an SM's registers)
+constexpr int kThreads = 384;    // threads per CTA of the plane kernels (two CTAs per SM: 24 warps)
 constexpr int kZThreads = 256;   // threads per CTA of the z-pencil kernel
 constexpr int kPlaneCap = 14336; // complex values of one shared-memory buffer (two are used)
 constexpr int kPlaneCapDefault = 7168;  // planner default: two CTAs per SM (measured faster)
@@ -144,7 +147,7 @@ struct EpiQuotient {
   __device__ __forceinline__ void operator()(long long g, float blurred) { q[g] = quotient(__ldg(img + g), blurred); }
   template <int K>
   __device__ __forceinline__ void apply(long long g0, const int* off, const float* val, const bool* ok) {
-    constexpr int C = K < 16 ? K : 16;
+    constexpr int C = K < 8 ? K : 8;
 #pragma unroll
     for (int c = 0; c < K; c += C) {
       float im[C];
@@ -200,7 +203,7 @@ struct EpiUpdate {
   }
   template <int K>
   __device__ __forceinline__ void apply(long long g0, const int* off, const float* val, const bool* ok) {
-    constexpr int C = K < 8 ? K : 8;  // voxels whose loads are in flight together
+    constexpr int C = K < 4 ? K : 4;
 #pragma unroll
     for (int c = 0; c < K; c += C) {
       float last[C], w[C];
@@ -274,7 +277,7 @@ struct EpiNll {
   }
   template <int K>
   __device__ __forceinline__ void apply(long long g0, const int* off, const float* val, const bool* ok) {
-    constexpr int C = K < 8 ? K : 8;
+    constexpr int C = K < 4 ? K : 4;
 #pragma unroll
     for (int c = 0; c < K; c += C) {
       float im[C], w[C];
@@ -397,6 +400,62 @@ struct OtfMul {  // v[r] *= OTF at natural index j + r NR of pencil `batch`
   }
 };
 
+// First column stage of the forward plane pass: the half spectrum X[y][kx] of the real rows,
+// formed on the fly from the packed row transforms Z (shared memory, rows of M complex):
+// X[k] = e - i w^k o with e = (Z[k] + conj Z[M-k]) / 2, o = (Z[k] - conj Z[M-k]) / 2,
+// X[0] = Re Z[0] + Im Z[0], X[M] = Re Z[0] - Im Z[0];  w = exp(-2 pi i / 2M).
+struct R2CColumnLoad {
+  const float2* z;
+  int pitch, M;
+  const float2* tw2;
+  template <int R>
+  __device__ __forceinline__ void get(int kx, int j, int NR, float2* v) const {
+    if (kx == 0 || kx == M) {
+      const float sg = kx == 0 ? 1.f : -1.f;
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        const float2 z0 = z[(j + r * NR) * pitch];
+        v[r] = make_float2(z0.x + sg * z0.y, 0.f);
+      }
+      return;
+    }
+    const float2 w = __ldg(tw2 + kx);
+    const int kc = M - kx;
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      const float2* row = z + (j + r * NR) * pitch;
+      const float2 zk = row[kx], zc = row[kc];
+      const float2 e = make_float2(0.5f * (zk.x + zc.x), 0.5f * (zk.y - zc.y));
+      const float2 o = make_float2(0.5f * (zk.x - zc.x), 0.5f * (zk.y + zc.y));
+      const float2 wo = cmul(w, o);
+      v[r] = make_float2(e.x + wo.y, e.y - wo.x);
+    }
+  }
+};
+
+// First row stage of the inverse plane pass: the packed transform Z[k] of effective row
+// `batch` formed from its half spectrum X (shared memory): Z[k] = (X[k] + conj X[M-k])
+// + i conj(w^k) (X[k] - conj X[M-k]); with an unnormalised inverse FFT_M it yields 2M x.
+struct C2RRowLoad {
+  const float2* x;  // effective row 0
+  int pitch, M;
+  const float2* tw2;
+  template <int R>
+  __device__ __forceinline__ void get(int batch, int j, int NR, float2* v) const {
+    const float2* row = x + batch * pitch;
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      const int k = j + r * NR;
+      const float2 xk = row[k], xc = row[k == 0 ? M : M - k];
+      const float2 e = make_float2(xk.x + xc.x, xk.y - xc.y);
+      const float2 o = make_float2(xk.x - xc.x, xk.y + xc.y);
+      const float2 w = k == 0 ? make_float2(1.f, 0.f) : __ldg(tw2 + k);
+      const float2 wo = cmul(cconj(w), o);
+      v[r] = make_float2(e.x - wo.y, e.y + wo.x);
+    }
+  }
+};
+
 template <class Epi>
 struct RowEpilogue {  // last inverse x stage: complex n of effective row `batch` = reals 2n, 2n+1
   Epi* epi;
@@ -424,9 +483,11 @@ struct RowEpilogue {  // last inverse x stage: complex n of effective row `batch
 
 // All stages of one transform with the result left in shared memory: on return (after a
 // barrier) `cur` holds it in the plain layout.  Stage 0 loads with ld0 (global memory or
-// `cur`) and every stage writes the other buffer.  ROWS (row transforms, es == 1): j-fastest
-// butterflies and the skewed layout between stages 0 and 1.
-template <bool INV, bool ROWS, class LD0>
+// `cur`) and every stage writes the other buffer.  ROWS (row transforms, es == 1): stage 0
+// (ROW_G0: it reads global memory) maps butterflies j-fastest for coalesced loads and writes
+// the skewed layout; exchanges between shared buffers map them batch-fastest (one position of
+// 32 consecutive rows per warp: conflict-free with an odd pitch).
+template <bool INV, bool ROWS, bool ROW_G0, class LD0>
 __device__ __forceinline__ void run_transform_smem(const FftPlan* __restrict__ p, int count, const LD0& ld0,
                                                    float2*& cur, float2*& oth, int es, int bs) {
   const int n = __ldg(&p->n);
@@ -435,12 +496,12 @@ __device__ __forceinline__ void run_transform_smem(const FftPlan* __restrict__ p
   int Ns = 1;
   for (int s = 0; s < ns; ++s) {
     const int R = __ldg(&p->radix[s]);
-    const int skew_out = (ROWS && s == 0 && ns > 1) ? -1 : 0;
-    const int skew_in = (ROWS && s == 1) ? -1 : 0;
+    const int skew_out = (ROWS && ROW_G0 && s == 0 && ns > 1) ? -1 : 0;
+    const int skew_in = (ROWS && ROW_G0 && s == 1) ? -1 : 0;
     if (s == 0)
-      stage<INV, ROWS>(R, n, Ns, count, tw, ld0, Smem{oth, es, bs, skew_out});
+      stage<INV, ROWS && ROW_G0>(R, n, Ns, count, tw, ld0, Smem{oth, es, bs, skew_out});
     else
-      stage<INV, ROWS>(R, n, Ns, count, tw, Smem{cur, es, bs, skew_in}, Smem{oth, es, bs, 0});
+      stage<INV, false>(R, n, Ns, count, tw, Smem{cur, es, bs, skew_in}, Smem{oth, es, bs, 0});
     __syncthreads();
     float2* t = cur;
     cur = oth;
@@ -451,6 +512,8 @@ __device__ __forceinline__ void run_transform_smem(const FftPlan* __restrict__ p
 
 // All stages of one transform with the last stage storing through `stl` (global memory or an
 // epilogue).  Stage 0 loads with ld0; the exchanges in between alternate the two buffers.
+// ROWS: the last stage (it writes global memory) maps butterflies j-fastest for coalesced
+// stores, reading the skewed layout; earlier stages map them batch-fastest.
 template <bool INV, bool ROWS, class LD0, class STL>
 __device__ __forceinline__ void run_transform_to(const FftPlan* __restrict__ p, int count, const LD0& ld0,
                                                  const STL& stl, float2*& cur, float2*& oth, int es, int bs) {
@@ -464,14 +527,14 @@ __device__ __forceinline__ void run_transform_to(const FftPlan* __restrict__ p, 
   int Ns = 1;
   for (int s = 0; s < ns; ++s) {
     const int R = __ldg(&p->radix[s]);
-    const int skew_in = (ROWS && s == 1) ? -1 : 0;
     if (s == ns - 1) {
-      stage<INV, ROWS>(R, n, Ns, count, tw, Smem{cur, es, bs, skew_in}, stl);
+      stage<INV, ROWS>(R, n, Ns, count, tw, Smem{cur, es, bs, ROWS ? -1 : 0}, stl);
     } else {
+      const int skew_out = (ROWS && s == ns - 2) ? -1 : 0;
       if (s == 0)
-        stage<INV, ROWS>(R, n, Ns, count, tw, ld0, Smem{oth, es, bs, ROWS ? -1 : 0});
+        stage<INV, false>(R, n, Ns, count, tw, ld0, Smem{oth, es, bs, skew_out});
       else
-        stage<INV, ROWS>(R, n, Ns, count, tw, Smem{cur, es, bs, skew_in}, Smem{oth, es, bs, 0});
+        stage<INV, false>(R, n, Ns, count, tw, Smem{cur, es, bs, 0}, Smem{oth, es, bs, skew_out});
       __syncthreads();
       float2* t = cur;
       cur = oth;
@@ -501,12 +564,12 @@ plane_fwd_kernel(const TileDesc* __restrict__ tiles, const int2* __restrict__ it
   RowGather<Gather, MASK> ld0{gather, t.ox, t.oy, t.oz + z, t.hx, t.hx + t.ex, t.hy, t.hy + t.ey,
                               z >= t.hz && z < t.hz + t.ez};
   const FftPlan* pxp = plans + t.plan_x;
-  run_transform_smem<false, true>(pxp, t.ty, ld0, cur, oth, 1, t.pitch);
-  r2c_post(cur, t.ty, M, t.pitch, pxp->tw_r2c);
-  __syncthreads();
-  // y: C2C of every column, last stage straight to the spectrum slice
+  run_transform_smem<false, true, true>(pxp, t.ty, ld0, cur, oth, 1, t.pitch);
+  // y: C2C of every half-spectrum column (formed while loading), last stage straight to the
+  // spectrum slice
   SpecSliceStore st{spec + t.spec_off + (long long)z * t.ty * t.px, t.px};
-  run_transform_to<false, false>(plans + t.plan_y, t.px, Smem{cur, t.pitch, 1, 0}, st, cur, oth, t.pitch, 1);
+  run_transform_to<false, false>(plans + t.plan_y, t.px, R2CColumnLoad{cur, t.pitch, M, pxp->tw_r2c}, st, cur, oth,
+                                 t.pitch, 1);
 }
 
 template <class Epi>
@@ -522,17 +585,18 @@ plane_inv_kernel(const TileDesc* __restrict__ tiles, const int2* __restrict__ it
   float2* oth = sm + t.ty * t.pitch;
   // y: inverse C2C of every column, first stage straight from the spectrum slice
   SpecSliceLoad ld{spec + t.spec_off + (long long)z * t.ty * t.px, t.px};
-  run_transform_smem<true, false>(plans + t.plan_y, t.px, ld, cur, oth, t.pitch, 1);
-  // only the effective rows go on: C2R pre-step and the inverse x transform
+  run_transform_smem<true, false, false>(plans + t.plan_y, t.px, ld, cur, oth, t.pitch, 1);
+  // only the effective rows go on: the inverse x transform, its first stage forming the
+  // packed transform of each row from the half spectrum while loading
   float2* rows = cur + t.hy * t.pitch;
   float2* rows_oth = oth + t.hy * t.pitch;
-  c2r_pre(rows, t.ey, M, t.pitch, plans[t.plan_x].tw_r2c);
-  __syncthreads();
+  const FftPlan* pxp = plans + t.plan_x;
   const long long gz = t.oz + z;
   RowEpilogue<Epi> st{&epi, (gz * epi.ny + (t.oy + t.hy)) * (long long)epi.nx + t.ox + t.hx, (long long)epi.nx,
                       t.hx, t.ex};
   epi.acc_init();
-  run_transform_to<true, true>(plans + t.plan_x, t.ey, Smem{rows, 1, t.pitch, 0}, st, rows, rows_oth, 1, t.pitch);
+  run_transform_to<true, true>(pxp, t.ey, C2RRowLoad{rows, t.pitch, M, pxp->tw_r2c}, st, rows, rows_oth, 1,
+                               t.pitch);
   epi.finish();
 }
 
