@@ -3,6 +3,8 @@
 // status code plus a per-thread message; nothing is retained across calls except in handles.
 #include <algorithm>
 #include <array>
+#include <chrono>
+#include <cstdlib>
 #include <cstdio>
 #include <map>
 #include <cstring>
@@ -107,6 +109,26 @@ struct DeviceCtx {
     auto& slot = otfs[key];
     slot = std::move(o);
     return slot.buf.as<float2>();
+  }
+};
+
+// MVD_TRACE=1 prints the duration of mvd_create's phases to stderr.
+struct PhaseTrace {
+  bool on;
+  std::chrono::steady_clock::time_point t0;
+  cudaStream_t s;
+  explicit PhaseTrace(cudaStream_t st) : s(st) {
+    const char* e = std::getenv("MVD_TRACE");
+    on = e && *e == '1';
+    t0 = std::chrono::steady_clock::now();
+  }
+  void mark(const char* what) {
+    if (!on) return;
+    cudaStreamSynchronize(s);
+    auto t1 = std::chrono::steady_clock::now();
+    std::fprintf(stderr, "[mvd_create] %-28s %8.2f ms\n", what,
+                 std::chrono::duration<double, std::milli>(t1 - t0).count());
+    t0 = t1;
   }
 };
 
@@ -664,8 +686,11 @@ extern "C" int mvd_create(mvd_decon** out, int devCUDA, const int* dims, int num
     h->k1[v].alloc(kb);
     MVD_CHECK(cudaMemcpyAsync(h->k1[v].p, psfs[v], kb, cudaMemcpyHostToDevice, h->stream));
   }
+  PhaseTrace trace(h->stream);
   MVD_CHECK(cudaStreamSynchronize(h->stream));
+  trace.mark("upload views/weights/psfs");
   prepare_kernels(h.get());
+  trace.mark("kernel preparation");
   h->psi.alloc(nb);
   h->q.alloc(nb);
   MVD_CHECK(cudaMemsetAsync(h->psi.p, 0, nb, h->stream));
@@ -691,6 +716,7 @@ extern "C" int mvd_create(mvd_decon** out, int devCUDA, const int* dims, int num
       h->plans.push_back(plan_view(h.get(), v, lo, hi, (flags & MVD_FLAG_AUTOTUNE) != 0));
     }
   }
+  trace.mark("data boxes and tile plans");
   for (int v = 0; v < num_views; ++v) {
     const ConvPlan& p = *h->plans[v];
     spec_max = std::max(spec_max, p.spec_elems);
@@ -701,6 +727,7 @@ extern "C" int mvd_create(mvd_decon** out, int devCUDA, const int* dims, int num
   }
   h->spec.alloc(spec_max * sizeof(float2));
   h->scratch.alloc(0);
+  trace.mark("kernel spectra (OTFs)");
   // first iteration: psi := average intensity of the overlapping area
   h->d_sc.alloc(2 * sizeof(double));
   MVD_CHECK(cudaMemsetAsync(h->d_sc.p, 0, 2 * sizeof(double), h->stream));
@@ -719,6 +746,7 @@ extern "C" int mvd_create(mvd_decon** out, int devCUDA, const int* dims, int num
   MVD_CHECK(cudaStreamSynchronize(h->stream));
   h->avg = sc[0] / sc[1];
   if (h->avg != h->avg) h->avg = 0.5;
+  trace.mark("first iteration, buffers");
   *out = h.release();
   return MVD_OK;
   MVD_API_END

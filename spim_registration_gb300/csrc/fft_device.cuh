@@ -253,18 +253,36 @@ struct ElemAccess {
 };
 
 // One radix-R Stockham stage of `count` sequences: ld.get<R>(...) and st.put<R>(...).
+// Butterflies b = tid, tid + T, ... are walked with an incremental (batch, j) (no integer
+// division in the loop) and k = j mod Ns is taken through an exact float reciprocal.
 template <int R, bool INV, bool JFAST, class LD, class ST>
 __device__ __forceinline__ void stage_r(int N, int Ns, int count, const float2* __restrict__ tw, const LD& ld,
                                         const ST& st) {
   const int NR = N / R;
   const int nb = count * NR;
   const int twstride = N / (Ns * R);
-  for (int b = threadIdx.x; b < nb; b += blockDim.x) {
-    int batch, j;
-    butterfly_index<JFAST>(b, count, NR, batch, j);
+  const int T = blockDim.x;
+  // fast and slow extents of the (batch, j) walk
+  const int fast = JFAST ? NR : count;
+  int f, sl;  // fast / slow coordinates of butterfly threadIdx.x
+  {
+    const int b = threadIdx.x;
+    sl = b / fast;
+    f = b - sl * fast;
+  }
+  const int dsl = T / fast, df = T - dsl * fast;
+  const float inv_ns = 1.0f / (float)Ns;
+  for (int b = threadIdx.x; b < nb; b += T) {
+    const int batch = JFAST ? sl : f;
+    const int j = JFAST ? f : sl;
     float2 v[R];
     ld.template get<R>(batch, j, NR, v);
-    const int k = j % Ns;
+    int k = 0;
+    if (Ns > 1) {
+      k = j - Ns * (int)((float)j * inv_ns);  // exact for j < 2^22 up to one step
+      if (k < 0) k += Ns;
+      if (k >= Ns) k -= Ns;
+    }
     if (k != 0) {
 #pragma unroll
       for (int r = 1; r < R; ++r) {
@@ -275,6 +293,12 @@ __device__ __forceinline__ void stage_r(int N, int Ns, int count, const float2* 
     }
     Dft<R, INV>::run(v);
     st.template put<R>(batch, (j - k) * R + k, Ns, v);
+    f += df;
+    sl += dsl;
+    if (f >= fast) {
+      f -= fast;
+      sl += 1;
+    }
   }
 }
 
@@ -350,11 +374,25 @@ struct Smem {
   __device__ __forceinline__ void operator()(int batch, int i, float2 v) const { p[at(batch, i)] = v; }
   template <int R>
   __device__ __forceinline__ void get(int batch, int j, int NR, float2* v) const {
-    ElemAccess::get<R>(*this, batch, j, NR, v);
+    if (skew) {
+      ElemAccess::get<R>(*this, batch, j, NR, v);
+    } else {  // base pointer and constant stride
+      const float2* q = p + batch * bs + j * es;
+      const int st = NR * es;
+#pragma unroll
+      for (int r = 0; r < R; ++r) v[r] = q[r * st];
+    }
   }
   template <int R>
   __device__ __forceinline__ void put(int batch, int base, int Ns, const float2* v) const {
-    ElemAccess::put<R>(*this, batch, base, Ns, v);
+    if (skew) {
+      ElemAccess::put<R>(*this, batch, base, Ns, v);
+    } else {
+      float2* q = p + batch * bs + base * es;
+      const int st = Ns * es;
+#pragma unroll
+      for (int r = 0; r < R; ++r) q[r * st] = v[r];
+    }
   }
 };
 
