@@ -4,6 +4,7 @@
 #include <algorithm>
 #include <array>
 #include <chrono>
+#include <climits>
 #include <cstdlib>
 #include <cstdio>
 #include <map>
@@ -466,28 +467,7 @@ struct mvd_decon {
 
 namespace {
 
-// small convolution with zero extension for kernel preparation
-DevBuf conv_zero(mvd_decon* h, const float* in, const std::array<int, 3>& d, const float* kern,
-                 const std::array<int, 3>& kd) {
-  auto plan = make_conv_plan(h->pt, d[0], d[1], d[2], kd[0], kd[1], kd[2]);
-  DevBuf otf(plan->otf_elems * sizeof(float2)), spec(plan->spec_elems * sizeof(float2));
-  DevBuf out((size_t)d[0] * d[1] * d[2] * sizeof(float));
-  build_otf(h->pt, *plan, kern, otf.as<float2>(), h->scratch, h->stream);
-  convolve(h->pt, *plan, in, Ext::Value, 0.f, otf.as<float2>(), spec.as<float2>(), out.as<float>(), h->stream);
-  MVD_CHECK(cudaStreamSynchronize(h->stream));
-  return out;
-}
-
 long long vox(const std::array<int, 3>& d) { return (long long)d[0] * d[1] * d[2]; }
-
-// AdjustInput.normImg with an FP64 unit-sum (AdjustInput.java:50-56)
-void norm_dev(mvd_decon* h, float* k, long long n) {
-  DevBuf sum(sizeof(double));
-  MVD_CHECK(cudaMemsetAsync(sum.p, 0, sizeof(double), h->stream));
-  dev_sum_f64(k, n, sum.as<double>(), h->stream);
-  dev_scale_div(k, n, sum.as<double>(), h->stream);
-  MVD_CHECK(cudaStreamSynchronize(h->stream));
-}
 
 DevBuf mirrored(mvd_decon* h, const float* k, const std::array<int, 3>& d) {
   DevBuf out(vox(d) * sizeof(float));
@@ -495,88 +475,83 @@ DevBuf mirrored(mvd_decon* h, const float* k, const std::array<int, 3>& d) {
   return out;
 }
 
-// MVDeconFFT.init (MVDeconFFT.java:183-324) for every view, on the GPU
+// MVDeconFFT.init (MVDeconFFT.java:183-324) for every view, on the GPU and asynchronous: the
+// PSF unit-sum normalisation in FP64 (AdjustInput.normImg, AdjustInput.java:50-56), the
+// mirrored kernels and the compound kernels, whose small convolutions use zero extension
+// (FFTConvolution over Views.extendZero, MVDeconFFT.java:222-248, 285-295).
 void prepare_kernels(mvd_decon* h) {
   const int V = h->V;
-  for (int v = 0; v < V; ++v) norm_dev(h, h->k1[v].as<float>(), vox(h->kd[v]));
+  cudaStream_t s = h->stream;
+  long long kmax = 0;
+  for (int v = 0; v < V; ++v) kmax = std::max(kmax, vox(h->kd[v]));
+  DevBuf A(kmax * sizeof(float)), B(kmax * sizeof(float)), C(kmax * sizeof(float)), sum(sizeof(double));
+  DevBuf otf, spec;
+  std::map<std::vector<int>, std::unique_ptr<ConvPlan>> plans;
+  auto norm = [&](float* k, long long n) {
+    MVD_CHECK(cudaMemsetAsync(sum.p, 0, sizeof(double), s));
+    dev_sum_f64(k, n, sum.as<double>(), s);
+    dev_scale_div(k, n, sum.as<double>(), s);
+  };
+  auto mirror = [&](const float* in, const std::array<int, 3>& d, float* out) {
+    dev_mirror(in, out, d[0], d[1], d[2], s);
+  };
+  // out = ext0(in) (*) kern over in's dims
+  auto conv0 = [&](const float* in, const std::array<int, 3>& d, const float* kern, const std::array<int, 3>& kd,
+                   float* out) {
+    const std::vector<int> key{d[0], d[1], d[2], kd[0], kd[1], kd[2]};
+    auto& plan = plans[key];
+    if (!plan) plan = make_conv_plan(h->pt, d[0], d[1], d[2], kd[0], kd[1], kd[2]);
+    otf.ensure(plan->otf_elems * sizeof(float2));
+    spec.ensure(plan->spec_elems * sizeof(float2));
+    build_otf(h->pt, *plan, kern, otf.as<float2>(), h->scratch, s);
+    convolve(h->pt, *plan, in, Ext::Value, 0.f, otf.as<float2>(), spec.as<float2>(), out, s);
+  };
+  for (int v = 0; v < V; ++v) norm(h->k1[v].as<float>(), vox(h->kd[v]));
   for (int v = 0; v < V; ++v) {
     const auto& dv = h->kd[v];
     const long long nv = vox(dv);
-    DevBuf k2;
+    h->k2[v].alloc(nv * sizeof(float));
+    float* k2 = h->k2[v].as<float>();
+    const float* k1 = h->k1[v].as<float>();
     if (V == 1 || h->psftype == MVD_INDEPENDENT) {
-      k2 = mirrored(h, h->k1[v].as<float>(), dv);
+      mirror(k1, dv, k2);
     } else if (h->psftype == MVD_EFFICIENT_BAYESIAN) {
-      DevBuf tmp = mirrored(h, h->k1[v].as<float>(), dv);
+      // P_v^compound = P_v* prod_{w != v} crop(crop(P_v* (*) P_w) (*) P_w*)
+      mirror(k1, dv, k2);
       for (int wv = 0; wv < V; ++wv) {
         if (wv == v) continue;
-        DevBuf in = mirrored(h, h->k1[v].as<float>(), dv);
-        DevBuf a = conv_zero(h, in.as<float>(), dv, h->k1[wv].as<float>(), h->kd[wv]);
-        DevBuf mw = mirrored(h, h->k1[wv].as<float>(), h->kd[wv]);
-        DevBuf b = conv_zero(h, a.as<float>(), dv, mw.as<float>(), h->kd[wv]);
-        dev_mul(tmp.as<float>(), b.as<float>(), nv, h->stream);
+        mirror(k1, dv, A.as<float>());
+        conv0(A.as<float>(), dv, h->k1[wv].as<float>(), h->kd[wv], B.as<float>());
+        mirror(h->k1[wv].as<float>(), h->kd[wv], C.as<float>());
+        conv0(B.as<float>(), dv, C.as<float>(), h->kd[wv], A.as<float>());
+        dev_mul(k2, A.as<float>(), nv, s);
       }
-      norm_dev(h, tmp.as<float>(), nv);
-      k2 = std::move(tmp);
+      norm(k2, nv);
     } else if (h->psftype == MVD_OPTIMIZATION_I) {
-      DevBuf tmp(nv * sizeof(float));
-      MVD_CHECK(cudaMemcpyAsync(tmp.p, h->k1[v].p, nv * sizeof(float), cudaMemcpyDeviceToDevice, h->stream));
+      // mirror(norm(P_v prod_{w != v} crop(P_v (*) P_w*)))
+      MVD_CHECK(cudaMemcpyAsync(A.p, k1, nv * sizeof(float), cudaMemcpyDeviceToDevice, s));
       for (int wv = 0; wv < V; ++wv) {
         if (wv == v) continue;
-        DevBuf mw = mirrored(h, h->k1[wv].as<float>(), h->kd[wv]);
-        DevBuf a = conv_zero(h, h->k1[v].as<float>(), dv, mw.as<float>(), h->kd[wv]);
-        dev_mul(tmp.as<float>(), a.as<float>(), nv, h->stream);
+        mirror(h->k1[wv].as<float>(), h->kd[wv], C.as<float>());
+        conv0(k1, dv, C.as<float>(), h->kd[wv], B.as<float>());
+        dev_mul(A.as<float>(), B.as<float>(), nv, s);
       }
-      norm_dev(h, tmp.as<float>(), nv);
-      k2 = mirrored(h, tmp.as<float>(), dv);
+      norm(A.as<float>(), nv);
+      mirror(A.as<float>(), dv, k2);
     } else {
-      DevBuf e(nv * sizeof(float));
-      MVD_CHECK(cudaMemcpyAsync(e.p, h->k1[v].p, nv * sizeof(float), cudaMemcpyDeviceToDevice, h->stream));
-      dev_pow(e.as<float>(), V, nv, h->stream);
-      norm_dev(h, e.as<float>(), nv);
-      k2 = mirrored(h, e.as<float>(), dv);
+      // OPTIMIZATION_II: mirror(norm(P_v ^ V))
+      MVD_CHECK(cudaMemcpyAsync(A.p, k1, nv * sizeof(float), cudaMemcpyDeviceToDevice, s));
+      dev_pow(A.as<float>(), V, nv, s);
+      norm(A.as<float>(), nv);
+      mirror(A.as<float>(), dv, k2);
     }
-    MVD_CHECK(cudaStreamSynchronize(h->stream));
-    h->k2[v] = std::move(k2);
   }
+  MVD_CHECK(cudaStreamSynchronize(s));  // the scratch buffers and plans go out of scope
 }
 
-// Bounding box of the voxels where a view has data (img > 0) or weight (w > 0).  Outside it
-// the quotient is 1 (MVDeconvolution.java:519-522) and the update leaves psi unchanged
-// (weight 0, :723), so a view's convolutions only need to cover this box.  An empty box
-// falls back to the whole volume.
-void data_box(const float* img, const float* w, const int* dims, int lo[3], int hi[3]) {
-  const int nx = dims[0], ny = dims[1], nz = dims[2];
-  int l[3] = {nx, ny, nz}, u[3] = {-1, -1, -1};
-  for (int z = 0; z < nz; ++z)
-    for (int y = 0; y < ny; ++y) {
-      const size_t row = ((size_t)z * ny + y) * nx;
-      int first = -1, last = -1;
-      for (int x = 0; x < nx; ++x)
-        if (img[row + x] > 0.f || w[row + x] > 0.f) {
-          if (first < 0) first = x;
-          last = x;
-        }
-      if (first < 0) continue;
-      l[0] = std::min(l[0], first);
-      u[0] = std::max(u[0], last);
-      l[1] = std::min(l[1], y);
-      u[1] = std::max(u[1], y);
-      l[2] = std::min(l[2], z);
-      u[2] = std::max(u[2], z);
-    }
-  for (int d = 0; d < 3; ++d) {
-    if (u[d] < 0) {  // no data at all
-      for (int e = 0; e < 3; ++e) {
-        lo[e] = 0;
-        hi[e] = dims[e];
-      }
-      return;
-    }
-    lo[d] = l[d];
-    hi[d] = u[d] + 1;
-  }
-}
-
+// A view's convolutions only need to cover the bounding box of its data or weight (img > 0
+// or w > 0): outside it the quotient is 1 (MVDeconvolution.java:519-522) and the update leaves
+// psi unchanged (weight 0, :723).  The boxes come from dev_data_box in mvd_create.
 // Tile plan of a view over its data box; with `autotune` the plane budgets below are all
 // tried and the fastest plan (one timed view stage each) is kept.
 std::unique_ptr<ConvPlan> plan_view(mvd_decon* h, int v, const int lo[3], const int hi[3], bool autotune) {
@@ -710,9 +685,27 @@ extern "C" int mvd_create(mvd_decon** out, int devCUDA, const int* dims, int num
     h->blk_in.alloc(blk_max * sizeof(float));
     h->blk_out.alloc(blk_max * sizeof(float));
   } else {
+    // data boxes of all views (GPU reduction), then one plan per view
+    std::vector<int> boxes(6 * num_views);
+    for (int v = 0; v < num_views; ++v) {
+      const int init[6] = {INT_MAX, INT_MAX, INT_MAX, -1, -1, -1};
+      std::copy(init, init + 6, boxes.begin() + 6 * v);
+    }
+    DevBuf d_boxes(boxes.size() * sizeof(int));
+    MVD_CHECK(cudaMemcpyAsync(d_boxes.p, boxes.data(), boxes.size() * sizeof(int), cudaMemcpyHostToDevice, h->stream));
+    for (int v = 0; v < num_views; ++v)
+      dev_data_box(h->img[v].as<float>(), h->w[v].as<float>(), dims[0], dims[1], dims[2], d_boxes.as<int>() + 6 * v,
+                   h->stream);
+    MVD_CHECK(cudaMemcpyAsync(boxes.data(), d_boxes.p, boxes.size() * sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    MVD_CHECK(cudaStreamSynchronize(h->stream));
     for (int v = 0; v < num_views; ++v) {
       int lo[3], hi[3];
-      data_box(views[v], weights[v], dims, lo, hi);
+      const int* b = boxes.data() + 6 * v;
+      const bool empty = b[3] < 0;  // no data and no weight: the whole volume (a no-op view)
+      for (int d = 0; d < 3; ++d) {
+        lo[d] = empty ? 0 : b[d];
+        hi[d] = empty ? dims[d] : b[3 + d] + 1;
+      }
       h->plans.push_back(plan_view(h.get(), v, lo, hi, (flags & MVD_FLAG_AUTOTUNE) != 0));
     }
   }

@@ -2,6 +2,7 @@
 // and the small elementwise / reduction kernels of the deconvolution path.
 #include <algorithm>
 #include <atomic>
+#include <climits>
 #include <cstdlib>
 #include <cmath>
 #include <cstring>
@@ -185,6 +186,24 @@ void ConvPlan::upload() {
   up(d_items_fwd, items_fwd);
   up(d_items_inv, items_inv);
   up(d_items_z, items_z);
+  // OTF build tables: one tile of this shape covering [0, T) with its full region effective
+  if (!tiles.empty()) {
+    TileDesc t = tiles[0];
+    t.ox = t.oy = t.oz = 0;
+    t.hx = t.hy = t.hz = 0;
+    t.ex = t.tx; t.ey = t.ty; t.ez = t.tz;
+    t.spec_off = 0;
+    t.otf_off = 0;
+    std::vector<int2> fwd, zz;
+    for (int z = 0; z < t.tz; ++z) fwd.push_back(make_int2(0, z));
+    for (int p0 = 0; p0 < t.ty * t.px; p0 += kZChunk) zz.push_back(make_int2(0, p0));
+    d_otf_tile.alloc(sizeof(TileDesc));
+    MVD_CHECK(cudaMemcpy(d_otf_tile.p, &t, sizeof(TileDesc), cudaMemcpyHostToDevice));
+    up(d_otf_fwd, fwd);
+    up(d_otf_z, zz);
+    n_otf_fwd = (int)fwd.size();
+    n_otf_z = (int)zz.size();
+  }
 }
 
 // Shared-memory budget of one plane buffer used by the planner (MVD_PLANE_CAP overrides it;
@@ -359,25 +378,10 @@ void build_otf(PlanTable& pt, const ConvPlan& plan, const float* kernel, float2*
   MVD_CHECK(cudaGetLastError());
   count_launch();
   // one tile covering the placed kernel volume exactly; its spectrum goes to `otf`
-  TileDesc t = plan.tiles[0];
-  t.ox = t.oy = t.oz = 0;
-  t.hx = t.hy = t.hz = 0;
-  t.ex = tx; t.ey = ty; t.ez = tz;
-  t.spec_off = 0;
-  t.otf_off = 0;
-  std::vector<int2> fwd, zz;
-  for (int z = 0; z < tz; ++z) fwd.push_back(make_int2(0, z));
-  for (int p0 = 0; p0 < ty * t.px; p0 += kZChunk) zz.push_back(make_int2(0, p0));
-  DevBuf dt(sizeof(TileDesc)), df(fwd.size() * sizeof(int2)), dz(zz.size() * sizeof(int2));
-  MVD_CHECK(cudaMemcpyAsync(dt.p, &t, sizeof(TileDesc), cudaMemcpyHostToDevice, s));
-  MVD_CHECK(cudaMemcpyAsync(df.p, fwd.data(), fwd.size() * sizeof(int2), cudaMemcpyHostToDevice, s));
-  MVD_CHECK(cudaMemcpyAsync(dz.p, zz.data(), zz.size() * sizeof(int2), cudaMemcpyHostToDevice, s));
-  launch_fwd_value_items(pt, plan, dt.as<TileDesc>(), df.as<int2>(), (int)fwd.size(), scratch.as<float>(), tx, ty, tz,
-                         0.f, otf, s);
-  launch_z_forward_scaled(pt, plan, dt.as<TileDesc>(), dz.as<int2>(), (int)zz.size(), otf,
+  launch_fwd_value_items(pt, plan, plan.d_otf_tile.as<TileDesc>(), plan.d_otf_fwd.as<int2>(), plan.n_otf_fwd,
+                         scratch.as<float>(), tx, ty, tz, 0.f, otf, s);
+  launch_z_forward_scaled(pt, plan, plan.d_otf_tile.as<TileDesc>(), plan.d_otf_z.as<int2>(), plan.n_otf_z, otf,
                           (float)(1.0 / ((double)tx * ty * tz)), s);
-  // the temporary tables are freed when this returns: wait for the launches that read them
-  MVD_CHECK(cudaStreamSynchronize(s));
 }
 
 // ------------------------------------------------------------------------------------------
@@ -638,6 +642,45 @@ void dev_paste_block(const float* block, int bx, int by, int bz, int lx, int ly,
   (void)nz;
   paste_block_kernel<<<grid_for((long long)sx * sy * sz), 256, 0, s>>>(block, bx, by, lx, ly, lz, vol, nx, ny, ex0,
                                                                      ey0, ez0, sx, sy, sz);
+  MVD_CHECK(cudaGetLastError());
+  count_launch();
+}
+
+__global__ void data_box_kernel(const float* __restrict__ img, const float* __restrict__ w, int nx, int ny, int nz,
+                                int* box) {
+  int lo[3] = {INT_MAX, INT_MAX, INT_MAX}, hi[3] = {-1, -1, -1};
+  const long long n = (long long)nx * ny * nz;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    if (__ldg(img + i) > 0.f || __ldg(w + i) > 0.f) {
+      const int c[3] = {(int)(i % nx), (int)((i / nx) % ny), (int)(i / ((long long)nx * ny))};
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        lo[d] = min(lo[d], c[d]);
+        hi[d] = max(hi[d], c[d]);
+      }
+    }
+  }
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      lo[d] = min(lo[d], __shfl_xor_sync(0xffffffffu, lo[d], o));
+      hi[d] = max(hi[d], __shfl_xor_sync(0xffffffffu, hi[d], o));
+    }
+  }
+  if ((threadIdx.x & 31) == 0) {
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      if (hi[d] >= 0) {
+        atomicMin(box + d, lo[d]);
+        atomicMax(box + 3 + d, hi[d]);
+      }
+    }
+  }
+}
+
+void dev_data_box(const float* img, const float* w, int nx, int ny, int nz, int* box, cudaStream_t s) {
+  data_box_kernel<<<grid_for((long long)nx * ny * nz), 256, 0, s>>>(img, w, nx, ny, nz, box);
   MVD_CHECK(cudaGetLastError());
   count_launch();
 }

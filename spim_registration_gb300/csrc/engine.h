@@ -79,6 +79,9 @@ struct ConvPlan {
   long long otf_elems = 0;             // complex elements of one OTF (all tiles share the shape)
   size_t smem_plane = 0, smem_z = 0;
   DevBuf d_tiles, d_items_fwd, d_items_inv, d_items_z;
+  // one tile of this shape at the origin and its work items: the OTF build's tables
+  DevBuf d_otf_tile, d_otf_fwd, d_otf_z;
+  int n_otf_fwd = 0, n_otf_z = 0;
   long long padded_voxels() const { return (long long)tiles.size() * ax.T * ay.T * az.T; }
   void upload();
 };
@@ -103,7 +106,8 @@ int plane_cap();
 std::string describe(const ConvPlan& p);
 
 // Build the (scaled) spectrum of a kernel for the tile shape of `plan` into `otf`
-// (plan.otf_elems complex values).  `kernel` is a device [kz][ky][kx] float array.
+// (plan.otf_elems complex values).  `kernel` is a device [kz][ky][kx] float array.  Enqueued
+// on `s` without waiting; `scratch_real` must stay allocated until the work is done.
 void build_otf(PlanTable& pt, const ConvPlan& plan, const float* kernel, float2* otf,
                DevBuf& scratch_real, cudaStream_t s);
 
@@ -168,6 +172,10 @@ void dev_fold_mirror(const float* c, int nxe, int nye, const int* tab, int nx, i
                      cudaStream_t s);
 // host: CSR tables of the mirror fold for an axis of n voxels extended by h on both sides
 void mirror_fold_table(int n, int h, std::vector<int>& start, std::vector<int>& idx);
+
+// bounding box of the voxels with img > 0 or w > 0: box[0..2] = min (x, y, z), box[3..5] = max
+// (atomics into `box`, which must hold {INT_MAX x3, -1 x3} before the call)
+void dev_data_box(const float* img, const float* w, int nx, int ny, int nz, int* box, cudaStream_t s);
 
 // ---- elementwise / reduction helpers (misc kernels) ----
 void dev_sum_f64(const float* x, long long n, double* out_dev, cudaStream_t s);  // *out += sum
