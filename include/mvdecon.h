@@ -169,6 +169,26 @@ int mvd_backward(mvd_decon* h, float* grad_psi, float* const* grad_psf);
  * as given (no normalisation), and its spectra -- e.g. after a projected gradient step. */
 int mvd_set_kernel(mvd_decon* h, int view, int which /* 1 or 2 */, const float* data);
 
+/* ----- input preparation (the views in the fused frame and their weights), on the GPU -----
+ * TransformInput.loop (spim/process/fusion/deconvolution/TransformInput.java:90-116) and
+ * TransformWeights with BlendingRealRandomAccess.computeWeight
+ * (spim/process/fusion/weights/BlendingRealRandomAccess.java:91-121).  For every voxel
+ * (x, y, z) of the fused output box (dims out_dims_xyz, global position + offset_xyz) the view
+ * position is t = affine^-1 (position), `affine` being the view's row-packed 3x4 registration
+ * (view -> world, imglib2 AffineTransform3D order).  out_img (may be NULL): trilinear value of
+ * the view extended mirror-single, clamped to >= 1e-4 where t lies inside the view, else 0
+ * ("no data").  out_blend (may be NULL): the cosine blending weight at t over the view's
+ * interval with border_xyz / blending_xyz.  Device pointers; enqueued on `stream`. */
+int mvd_transform_view(const float* view, const int* view_dims_xyz, const double* affine, const int* offset_xyz,
+                       const int* out_dims_xyz, float* out_img, float* out_blend, const float* border_xyz,
+                       const float* blending_xyz, int devCUDA, void* stream);
+/* WeightNormalizer's VIRTUAL normalisation with the OSEM factor, in place on `num_views`
+ * device weight volumes of n voxels: w_v / (sum_w > 1 ? sum_w : 1), then min(1, w * osem)
+ * (WeightNormalizer.java:73-253, NormalizingRandomAccess.java:57-66,
+ * ProcessForDeconvolution.java:372-405). */
+int mvd_normalize_weights(float* const* weights, int num_views, long long n, double osem, int devCUDA,
+                          void* stream);
+
 #ifdef __cplusplus
 }
 #endif

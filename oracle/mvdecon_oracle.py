@@ -457,3 +457,76 @@ def poisson_nll_grad(psi, views, weights, psfs):
                     g[jz, jy, jx] = np.sum(r * pe[oz:oz + nz, oy:oy + ny, ox:ox + nx])
         g_psf.append(g)
     return g_psi, g_psf
+
+
+# --------------------------------------------------------------------------------------------
+# input preparation: views in the fused frame, blending weights, VIRTUAL normalisation
+# --------------------------------------------------------------------------------------------
+def _inverse_affine(affine_rows):
+    a = np.asarray(affine_rows, dtype=np.float64).reshape(3, 4)
+    r_inv = np.linalg.inv(a[:, :3])
+    return r_inv, -r_inv @ a[:, 3]
+
+
+def _view_positions(affine_rows, offset_xyz, out_shape_zyx):
+    nz, ny, nx = out_shape_zyx
+    z, y, x = np.meshgrid(np.arange(nz), np.arange(ny), np.arange(nx), indexing="ij")
+    s = np.stack([x + offset_xyz[0], y + offset_xyz[1], z + offset_xyz[2]], axis=-1).astype(np.float64)
+    r_inv, t = _inverse_affine(affine_rows)
+    return s @ r_inv.T + t  # (..., 3) view coordinates (x, y, z)
+
+
+def transform_input(view, affine_rows, offset_xyz, out_shape_zyx):
+    """TransformInput.loop (TransformInput.java:90-116), FP64: trilinear interpolation of the
+    mirror-single extended view at affine^-1(position); max(minValue, .) inside the view, 0
+    outside (FusionHelper.intersects, FusionHelper.java:75-81)."""
+    v = np.asarray(view, dtype=np.float64)
+    sz, sy, sx = v.shape
+    t = _view_positions(affine_rows, offset_xyz, out_shape_zyx)
+    f = np.floor(t)
+    a = t - f
+    i0 = f.astype(np.int64)
+    out = np.zeros(t.shape[:-1])
+    for c in range(8):
+        bx, by, bz = c & 1, (c >> 1) & 1, (c >> 2) & 1
+        xi = mirror_single_index(i0[..., 0] + bx, sx)
+        yi = mirror_single_index(i0[..., 1] + by, sy)
+        zi = mirror_single_index(i0[..., 2] + bz, sz)
+        w = (a[..., 0] if bx else 1 - a[..., 0]) * (a[..., 1] if by else 1 - a[..., 1]) * (a[..., 2] if bz else 1 - a[..., 2])
+        out += w * v[zi, yi, xi]
+    inside = (t[..., 0] >= 0) & (t[..., 1] >= 0) & (t[..., 2] >= 0) & (t[..., 0] < sx) & (t[..., 1] < sy) & (t[..., 2] < sz)
+    return np.where(inside, np.maximum(float(MIN_VALUE), out), 0.0)
+
+
+_BLEND_LUT = np.array([(math.cos((1 - k / 1000.0) * math.pi) + 1) / 2 for k in range(1001)])
+
+
+def transform_weights(view_shape_zyx, affine_rows, offset_xyz, out_shape_zyx, border_xyz, blending_xyz):
+    """TransformWeights + BlendingRealRandomAccess.computeWeight (BlendingRealRandomAccess.java:
+    44-121): the cosine blending weight at affine^-1(position) over the view interval, with
+    the 1001-entry lookup table (index round(d * 1000))."""
+    sz, sy, sx = view_shape_zyx
+    t = _view_positions(affine_rows, offset_xyz, out_shape_zyx).astype(np.float32)
+    dm1 = (sx - 1, sy - 1, sz - 1)
+    w = np.ones(t.shape[:-1], dtype=np.float32)
+    zero = np.zeros(t.shape[:-1], dtype=bool)
+    for d in range(3):
+        l = t[..., d]
+        dist = np.maximum(np.float32(0), np.minimum(l - np.float32(border_xyz[d]),
+                                                    np.float32(dm1[d]) - l - np.float32(border_xyz[d])))
+        zero |= dist == 0
+        rel = (dist / np.float32(blending_xyz[d])).astype(np.float32)
+        idx = np.floor(rel.astype(np.float64) * 1000.0 + 0.5).astype(np.int64)
+        lut = _BLEND_LUT[np.clip(idx, 0, 1000)]
+        w = np.where(rel < 1, (w.astype(np.float64) * lut).astype(np.float32), w)
+    return np.where(zero, np.float32(0), w).astype(np.float32)
+
+
+def normalize_weights_virtual(weights, osem=1.0):
+    """VIRTUAL weights (WeightNormalizer.java:73-253, NormalizingRandomAccess.java:57-66):
+    w_v / (sum > 1 ? (float)sum : 1), then min(1, w * osem)."""
+    s = np.zeros(weights[0].shape, dtype=np.float64)
+    for w in weights:
+        s += w.astype(np.float64)
+    norm = np.where(s > 1, s.astype(np.float32), np.float32(1)).astype(np.float64)
+    return [np.minimum(1.0, w.astype(np.float64) / norm * osem).astype(np.float32) for w in weights]

@@ -17,7 +17,7 @@ CSRC = os.path.join(PKG, "csrc")
 LIBDIR = os.path.join(PKG, "lib")
 LIBNAME = "libFourierConvolutionCUDA.so"
 ALIAS = "libConvolution3D_fftCUDAlib.so"
-SOURCES = ["engine.cu", "passes_fwd.cu", "passes_inv.cu", "passes_z.cu", "adjoint.cu", "capi.cu", "noalloc.cu"]
+SOURCES = ["engine.cu", "passes_fwd.cu", "passes_inv.cu", "passes_z.cu", "adjoint.cu", "inputs.cu", "capi.cu", "noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2", "-Xptxas", "-O3"]
 

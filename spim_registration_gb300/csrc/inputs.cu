@@ -1,0 +1,239 @@
+// Input preparation of the deconvolution on the GPU: every view resampled into the fused box
+// with its blending weight, and the VIRTUAL weight normalisation with the OSEM factor.
+//   TransformInput.loop         spim/process/fusion/deconvolution/TransformInput.java:90-116
+//   TransformWeights.call       spim/process/fusion/deconvolution/TransformWeights.java
+//   BlendingRealRandomAccess    spim/process/fusion/weights/BlendingRealRandomAccess.java:44-121
+//   WeightNormalizer (VIRTUAL)  spim/process/fusion/deconvolution/WeightNormalizer.java:73-253,
+//                               spim/process/fusion/weights/NormalizingRandomAccess.java:57-66
+//   OSEM factor                 ProcessForDeconvolution.java:372-405
+#include <cmath>
+#include <cstring>
+#include <string>
+
+#include "../../include/mvdecon.h"
+#include "engine.h"
+
+using namespace mvd;
+
+namespace mvd {
+void set_last_error(const std::string& msg);
+}
+
+namespace {
+
+struct Affine {  // world -> view (the inverse of the view's registration), row-packed 3x4
+  float m[12];
+};
+
+// BlendingRealRandomAccess's 1001-entry lookup table of (cos((1 - d) pi) + 1) / 2
+__constant__ double c_blend_lut[1001];
+
+__device__ __forceinline__ int mirror_single_i(int i, int n) {
+  if (i >= 0 && i < n) return i;
+  if (n == 1) return 0;
+  const int period = 2 * n - 2;
+  int m = i % period;
+  if (m < 0) m += period;
+  return m < n ? m : period - m;
+}
+
+// NLinearInterpolator over Views.extendMirrorSingle(img) at the real position t
+__device__ __forceinline__ float trilinear_mirror(const float* __restrict__ img, int sx, int sy, int sz, float tx,
+                                                  float ty, float tz) {
+  const float fx0 = floorf(tx), fy0 = floorf(ty), fz0 = floorf(tz);
+  const int x0 = (int)fx0, y0 = (int)fy0, z0 = (int)fz0;
+  const float ax = tx - fx0, ay = ty - fy0, az = tz - fz0;
+  const int xs[2] = {mirror_single_i(x0, sx), mirror_single_i(x0 + 1, sx)};
+  const int ys[2] = {mirror_single_i(y0, sy), mirror_single_i(y0 + 1, sy)};
+  const int zs[2] = {mirror_single_i(z0, sz), mirror_single_i(z0 + 1, sz)};
+  float acc = 0.f;
+#pragma unroll
+  for (int c = 0; c < 8; ++c) {
+    const int bx = c & 1, by = (c >> 1) & 1, bz = (c >> 2) & 1;
+    const float w = (bx ? ax : 1.f - ax) * (by ? ay : 1.f - ay) * (bz ? az : 1.f - az);
+    acc += w * __ldg(img + ((long long)zs[bz] * sy + ys[by]) * sx + xs[bx]);
+  }
+  return acc;
+}
+
+// BlendingRealRandomAccess.computeWeight (:91-121) on the view interval [0, size)
+__device__ __forceinline__ float blend_weight(float lx, float ly, float lz, int sx, int sy, int sz, float3 border,
+                                              float3 range) {
+  const float loc[3] = {lx, ly, lz};
+  const float dm1[3] = {(float)(sx - 1), (float)(sy - 1), (float)(sz - 1)};
+  const float b[3] = {border.x, border.y, border.z};
+  const float r[3] = {range.x, range.y, range.z};
+  float w = 1.f;
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    const float l = loc[d];
+    const float dist = fmaxf(0.f, fminf(l - b[d], dm1[d] - l - b[d]));
+    if (dist == 0.f) return 0.f;
+    const float rel = dist / r[d];
+    if (rel < 1.f) {
+      // indexFor(d) = Math.round(d * 1000.0)
+      const int idx = (int)floor((double)rel * 1000.0 + 0.5);
+      w = (float)((double)w * c_blend_lut[idx]);
+    }
+  }
+  return w;
+}
+
+__global__ void transform_view_kernel(const float* __restrict__ view, int sx, int sy, int sz, Affine inv, int ox,
+                                      int oy, int oz, int nx, int ny, int nz, float* __restrict__ out_img,
+                                      float* __restrict__ out_blend, float3 border, float3 range) {
+  const long long n = (long long)nx * ny * nz;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const int x = (int)(i % nx), y = (int)((i / nx) % ny), z = (int)(i / ((long long)nx * ny));
+    const float s0 = (float)(x + ox), s1 = (float)(y + oy), s2 = (float)(z + oz);
+    const float t0 = inv.m[0] * s0 + inv.m[1] * s1 + inv.m[2] * s2 + inv.m[3];
+    const float t1 = inv.m[4] * s0 + inv.m[5] * s1 + inv.m[6] * s2 + inv.m[7];
+    const float t2 = inv.m[8] * s0 + inv.m[9] * s1 + inv.m[10] * s2 + inv.m[11];
+    if (out_img) {
+      float v = 0.f;  // no image data (MVDeconvolution.computeQuotient reads 0 as "no data")
+      if (t0 >= 0.f && t1 >= 0.f && t2 >= 0.f && t0 < (float)sx && t1 < (float)sy && t2 < (float)sz)
+        v = fmaxf(1e-4f, trilinear_mirror(view, sx, sy, sz, t0, t1, t2));
+      out_img[i] = v;
+    }
+    // the blending weight is defined everywhere (the border can be negative)
+    if (out_blend) out_blend[i] = blend_weight(t0, t1, t2, sx, sy, sz, border, range);
+  }
+}
+
+struct WeightPtrs {
+  float* p[16];
+};
+
+// VIRTUAL: w_v / (sum_w > 1 ? sum_w : 1) (sum in double, the normaliser stored as float),
+// then min(1, w * osem)
+__global__ void normalize_weights_kernel(WeightPtrs w, int nv, long long n, double osem) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    double sum = 0.0;
+    for (int v = 0; v < nv; ++v) sum += (double)w.p[v][i];
+    const float norm = sum > 1.0 ? (float)sum : 1.f;
+    for (int v = 0; v < nv; ++v) {
+      const double x = (double)w.p[v][i] / (double)norm;
+      w.p[v][i] = (float)fmin(1.0, x * osem);
+    }
+  }
+}
+
+int grid_n(long long n) {
+  long long b = (n + 255) / 256;
+  return (int)(b < 1 ? 1 : (b > 152LL * 32 ? 152LL * 32 : b));
+}
+
+bool g_lut_ready[64] = {};
+
+void upload_lut(int dev) {
+  if (dev < 64 && g_lut_ready[dev]) return;
+  double lut[1001];
+  // the reference fills the table by stepping d in 0.001 increments; index k holds the value
+  // of d = k / 1000 (to within the accumulated rounding of the step)
+  for (int k = 0; k <= 1000; ++k) lut[k] = (std::cos((1.0 - k / 1000.0) * M_PI) + 1.0) / 2.0;
+  MVD_CHECK(cudaMemcpyToSymbol(c_blend_lut, lut, sizeof(lut)));
+  if (dev < 64) g_lut_ready[dev] = true;
+}
+
+bool invert_affine(const double* a, Affine& out) {
+  // a: row-packed 3x4 [R | t] (view -> world); inverse = [R^-1 | -R^-1 t]
+  const double r00 = a[0], r01 = a[1], r02 = a[2], r10 = a[4], r11 = a[5], r12 = a[6], r20 = a[8], r21 = a[9],
+               r22 = a[10];
+  const double det = r00 * (r11 * r22 - r12 * r21) - r01 * (r10 * r22 - r12 * r20) + r02 * (r10 * r21 - r11 * r20);
+  if (!(std::fabs(det) > 0.0)) return false;
+  double inv[9] = {(r11 * r22 - r12 * r21) / det, (r02 * r21 - r01 * r22) / det, (r01 * r12 - r02 * r11) / det,
+                   (r12 * r20 - r10 * r22) / det, (r00 * r22 - r02 * r20) / det, (r02 * r10 - r00 * r12) / det,
+                   (r10 * r21 - r11 * r20) / det, (r01 * r20 - r00 * r21) / det, (r00 * r11 - r01 * r10) / det};
+  const double t[3] = {a[3], a[7], a[11]};
+  for (int r = 0; r < 3; ++r) {
+    for (int c = 0; c < 3; ++c) out.m[4 * r + c] = (float)inv[3 * r + c];
+    out.m[4 * r + 3] = (float)-(inv[3 * r] * t[0] + inv[3 * r + 1] * t[1] + inv[3 * r + 2] * t[2]);
+  }
+  return true;
+}
+
+}  // namespace
+
+extern "C" int mvd_transform_view(const float* view, const int* vd, const double* affine, const int* offset,
+                                  const int* od, float* out_img, float* out_blend, const float* border,
+                                  const float* blending, int devCUDA, void* stream) {
+  try {
+    set_last_error("");
+    if (!view || !vd || !affine || !offset || !od || (!out_img && !out_blend)) {
+      set_last_error("NULL argument");
+      return MVD_ERR_ARG;
+    }
+    if (out_blend && (!border || !blending)) {
+      set_last_error("blending weights need border and blending sizes");
+      return MVD_ERR_ARG;
+    }
+    for (int d = 0; d < 3; ++d) {
+      if (vd[d] < 1 || od[d] < 1) {
+        set_last_error("sizes must be positive");
+        return MVD_ERR_ARG;
+      }
+      if (out_blend && !(blending[d] > 0.f)) {
+        set_last_error("blending sizes must be positive");
+        return MVD_ERR_ARG;
+      }
+    }
+    Affine inv;
+    if (!invert_affine(affine, inv)) {
+      set_last_error("the affine transform is singular");
+      return MVD_ERR_ARG;
+    }
+    int count = 0;
+    MVD_CHECK(cudaGetDeviceCount(&count));
+    if (devCUDA < 0 || devCUDA >= count) {
+      set_last_error("invalid CUDA device id");
+      return MVD_ERR_ARG;
+    }
+    MVD_CHECK(cudaSetDevice(devCUDA));
+    upload_lut(devCUDA);
+    const long long n = (long long)od[0] * od[1] * od[2];
+    const float3 b = out_blend ? make_float3(border[0], border[1], border[2]) : make_float3(0.f, 0.f, 0.f);
+    const float3 r = out_blend ? make_float3(blending[0], blending[1], blending[2]) : make_float3(1.f, 1.f, 1.f);
+    transform_view_kernel<<<grid_n(n), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+        view, vd[0], vd[1], vd[2], inv, offset[0], offset[1], offset[2], od[0], od[1], od[2], out_img, out_blend, b, r);
+    MVD_CHECK(cudaGetLastError());
+    count_launch();
+    return MVD_OK;
+  } catch (const CudaError& e) {
+    set_last_error(e.what());
+    return MVD_ERR_CUDA;
+  } catch (const std::exception& e) {
+    set_last_error(e.what());
+    return MVD_ERR_INTERNAL;
+  }
+}
+
+extern "C" int mvd_normalize_weights(float* const* weights, int num_views, long long n, double osem, int devCUDA,
+                                     void* stream) {
+  try {
+    set_last_error("");
+    if (!weights || num_views < 1 || num_views > 16 || n < 0) {
+      set_last_error("bad arguments (1..16 weight volumes)");
+      return MVD_ERR_ARG;
+    }
+    WeightPtrs wp{};
+    for (int v = 0; v < num_views; ++v) {
+      if (!weights[v]) {
+        set_last_error("NULL weight volume");
+        return MVD_ERR_ARG;
+      }
+      wp.p[v] = weights[v];
+    }
+    MVD_CHECK(cudaSetDevice(devCUDA));
+    if (n == 0) return MVD_OK;
+    normalize_weights_kernel<<<grid_n(n), 256, 0, static_cast<cudaStream_t>(stream)>>>(wp, num_views, n, osem);
+    MVD_CHECK(cudaGetLastError());
+    count_launch();
+    return MVD_OK;
+  } catch (const CudaError& e) {
+    set_last_error(e.what());
+    return MVD_ERR_CUDA;
+  } catch (const std::exception& e) {
+    set_last_error(e.what());
+    return MVD_ERR_INTERNAL;
+  }
+}

@@ -73,6 +73,10 @@ SIGNATURES = {
     "mvd_forward": (ctypes.c_int, [_H, _D]),
     "mvd_backward": (ctypes.c_int, [_H, _F, ctypes.POINTER(_F)]),
     "mvd_set_kernel": (ctypes.c_int, [_H, ctypes.c_int, ctypes.c_int, _F]),
+    "mvd_transform_view": (ctypes.c_int, [ctypes.c_void_p, _I, _D, _I, _I, ctypes.c_void_p, ctypes.c_void_p, _F, _F,
+                                          ctypes.c_int, ctypes.c_void_p]),
+    "mvd_normalize_weights": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int, ctypes.c_longlong,
+                                             ctypes.c_double, ctypes.c_int, ctypes.c_void_p]),
 }
 
 

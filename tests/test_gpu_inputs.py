@@ -1,0 +1,85 @@
+"""Input preparation on the GPU against the oracle: a view resampled into the fused box
+(TransformInput), its blending weight (TransformWeights + BlendingRealRandomAccess) and the
+VIRTUAL weight normalisation with the OSEM factor (WeightNormalizer).
+
+The GPU evaluates the inverse transform in float, the oracle in double, so voxels whose view
+position lies within 1e-3 of the view's border (the inside test) are left out of the value
+comparison; the blending lookup table is piecewise constant in steps of 0.001, so weights are
+compared to 3e-3 absolute (most are identical).
+"""
+import math
+
+import numpy as np
+import pytest
+
+from oracle import mvdecon_oracle as O
+from spim_registration_gb300 import native
+
+pytestmark = pytest.mark.gpu
+
+
+def _affine(angle_deg, scale_xyz, shift_xyz):
+    t = math.radians(angle_deg)
+    c, s = math.cos(t), math.sin(t)
+    rot = np.array([[c, 0, s], [0, 1, 0], [-s, 0, c]])
+    m = rot @ np.diag(scale_xyz)
+    return np.concatenate([m, np.asarray(shift_xyz, dtype=np.float64)[:, None]], axis=1).ravel()
+
+
+@pytest.mark.parametrize("angle,scale", [(0.0, (1, 1, 1)), (30.0, (1, 1, 2.0)), (90.0, (1.0, 1.0, 1.5))])
+def test_transform_view_matches_oracle(angle, scale):
+    torch = pytest.importorskip("torch")
+    lib = native.load()
+    rng = np.random.default_rng(3)
+    view = (rng.random((18, 22, 26)) * 100 + 1).astype(np.float32)  # z, y, x
+    affine = _affine(angle, scale, (14.25, 3.375, 9.125))  # fractional: no position exactly on the border
+    out_shape = (40, 30, 44)  # z, y, x
+    offset = (-6, -2, -5)
+    border, blend = (-8.0, -8.0, -3.0), (12.0, 12.0, 12.0)
+    dv = torch.from_numpy(view).cuda()
+    oimg = torch.full(out_shape, float("nan"), device="cuda")
+    oblend = torch.full(out_shape, float("nan"), device="cuda")
+    st = lib.mvd_transform_view(dv.data_ptr(), native.iarr([26, 22, 18]), (native.ctypes.c_double * 12)(*affine),
+                                native.iarr(offset), native.iarr([44, 30, 40]), oimg.data_ptr(), oblend.data_ptr(),
+                                (native.ctypes.c_float * 3)(*border), (native.ctypes.c_float * 3)(*blend), 0, None)
+    native.check(st)
+    torch.cuda.synchronize()
+    got = oimg.cpu().numpy().astype(np.float64)
+    want = O.transform_input(view, affine, offset, out_shape)
+    t = O._view_positions(affine, offset, out_shape)
+    size = np.array([26, 22, 18])
+    margin = np.minimum(np.abs(t), np.abs(t - size)).min(axis=-1)
+    safe = margin > 1e-3
+    assert safe.mean() > 0.9
+    inside = want > 0
+    assert inside[safe].any() and (~inside[safe]).any() or angle == 0.0
+    assert np.array_equal(got[safe] > 0, inside[safe])
+    rel = np.abs(got - want)[safe].max() / np.abs(want).max()
+    assert rel < 1e-5, rel
+    wb = O.transform_weights(view.shape, affine, offset, out_shape, border, blend)
+    gb = oblend.cpu().numpy()
+    assert np.isfinite(gb).all()
+    assert np.abs(gb - wb).max() < 3e-3
+    assert np.mean(gb == wb) > 0.98
+
+
+@pytest.mark.parametrize("osem", [1.0, 1.7])
+def test_normalize_weights_matches_oracle(osem):
+    torch = pytest.importorskip("torch")
+    lib = native.load()
+    rng = np.random.default_rng(4)
+    ws = [np.where(rng.random((20, 16, 12)) < 0.2, 0, rng.random((20, 16, 12))).astype(np.float32) for _ in range(3)]
+    want = O.normalize_weights_virtual(ws, osem)
+    dws = [torch.from_numpy(w).cuda() for w in ws]
+    ptrs = (native.ctypes.c_void_p * 3)(*[d.data_ptr() for d in dws])
+    native.check(lib.mvd_normalize_weights(ptrs, 3, ws[0].size, osem, 0, None))
+    torch.cuda.synchronize()
+    for d, w in zip(dws, want):
+        np.testing.assert_allclose(d.cpu().numpy(), w, rtol=2e-7, atol=0)
+
+
+def test_transform_view_rejects_singular_affines():
+    lib = native.load()
+    st = lib.mvd_transform_view(1, native.iarr([4, 4, 4]), (native.ctypes.c_double * 12)(*([0.0] * 12)),
+                                native.iarr([0, 0, 0]), native.iarr([4, 4, 4]), 1, None, None, None, 0, None)
+    assert st == 1 and "singular" in lib.mvd_last_error().decode()

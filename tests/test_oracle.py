@@ -183,3 +183,39 @@ def test_nll_gradient_matches_central_differences():
         b[v][i] -= 1e-5
         fd = (O.poisson_nll(psi, p.views, p.weights, a) - O.poisson_nll(psi, p.views, p.weights, b)) / 2e-5
         assert gk[v][i] == pytest.approx(fd, rel=1e-4)
+
+
+def test_transform_input_identity_and_shift():
+    rng = np.random.default_rng(11)
+    view = (rng.random((6, 7, 8)) * 10 + 1).astype(np.float32)
+    eye = [1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0]
+    np.testing.assert_allclose(O.transform_input(view, eye, (0, 0, 0), view.shape), view, rtol=1e-12)
+    # a registration shift of +2 in x moves the view to x >= 2 of the fused box; left of it is "no data"
+    shifted = [1, 0, 0, 2, 0, 1, 0, 0, 0, 0, 1, 0]
+    out = O.transform_input(view, shifted, (0, 0, 0), (6, 7, 10))
+    np.testing.assert_allclose(out[:, :, 2:], view, rtol=1e-12)
+    assert np.all(out[:, :, :2] == 0)
+
+
+def test_blending_weights_profile():
+    # along x: 0 at the border, cosine ramp over `blending` voxels, 1 in the middle
+    eye = [1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0]
+    w = O.transform_weights((9, 9, 41), eye, (0, 0, 0), (9, 9, 41), (0.0, -20.0, -20.0), (10.0, 1.0, 1.0))
+    row = w[4, 4]
+    assert row[0] == 0 and row[-1] == 0
+    assert np.all(np.diff(row[:11]) >= 0) and np.all(row[10:31] == 1)
+    np.testing.assert_allclose(row, row[::-1], atol=1e-6)
+    assert row[5] == pytest.approx(0.5, abs=1e-6)
+
+
+def test_virtual_weight_normalisation():
+    rng = np.random.default_rng(12)
+    ws = [rng.random((5, 6, 7)).astype(np.float32) * 0.9 for _ in range(4)]
+    n1 = O.normalize_weights_virtual(ws, 1.0)
+    s = np.sum(n1, axis=0)
+    assert np.all(s <= 1 + 1e-6)
+    big = np.sum(ws, axis=0) > 1
+    np.testing.assert_allclose(s[big], 1, rtol=1e-5)
+    np.testing.assert_allclose(n1[0][~big], ws[0][~big], rtol=1e-7)
+    n2 = O.normalize_weights_virtual(ws, 3.0)
+    assert np.all(n2[0] <= 1) and np.all(n2[0] >= np.minimum(1, n1[0] * 3 * (1 - 1e-6)))
