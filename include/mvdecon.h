@@ -107,7 +107,9 @@ int mvd_convolve3d_device_noalloc(const float* in, float* out, const int* dims_x
  * of the first iteration (MVDeconvolution.java:133-147).  Each view's convolutions cover only
  * the bounding box of its data (img > 0 or weight > 0), with all of its tiles, of whatever
  * shape, in one launch per pass.  block_xyz selects the reference's block size for
- * MVD_FLAG_PLAIN (NULL = one block of image + kernel - 1). */
+ * MVD_FLAG_PLAIN (NULL = one block of image + kernel - 1).  views, weights and psfs may point
+ * to host memory or to device memory of devCUDA (copied on the handle's own stream: work that
+ * writes them on another stream must be complete before the call). */
 typedef struct mvd_decon mvd_decon;
 
 int mvd_create(mvd_decon** out, int devCUDA, const int* dims_xyz, int num_views,
@@ -182,12 +184,21 @@ int mvd_set_kernel(mvd_decon* h, int view, int which /* 1 or 2 */, const float* 
 int mvd_transform_view(const float* view, const int* view_dims_xyz, const double* affine, const int* offset_xyz,
                        const int* out_dims_xyz, float* out_img, float* out_blend, const float* border_xyz,
                        const float* blending_xyz, int devCUDA, void* stream);
-/* WeightNormalizer's VIRTUAL normalisation with the OSEM factor, in place on `num_views`
- * device weight volumes of n voxels: w_v / (sum_w > 1 ? sum_w : 1), then min(1, w * osem)
- * (WeightNormalizer.java:73-253, NormalizingRandomAccess.java:57-66,
- * ProcessForDeconvolution.java:372-405). */
-int mvd_normalize_weights(float* const* weights, int num_views, long long n, double osem, int devCUDA,
+/* WeightNormalizer's normalisation with the OSEM factor, in place on `num_views` device weight
+ * volumes of n voxels (WeightNormalizer.java:73-253, ProcessForDeconvolution.java:372-405).
+ * mode 0, VIRTUAL (NormalizingRandomAccess.java:57-66): w_v / (sum_w > 1 ? sum_w : 1), then
+ * min(1, w * osem).  mode 1, PRECOMPUTED (WeightNormalizer.ApplyDirectly): w_v / sum_w, then
+ * min(1, w * (float)osem); NaN where no view has weight, as in the reference. */
+int mvd_normalize_weights(float* const* weights, int num_views, long long n, double osem, int mode, int devCUDA,
                           void* stream);
+/* WeightNormalizer's overlap statistics (WeightNormalizer.java:94-106, 187-252), which
+ * ProcessForDeconvolution uses as the automatic OSEM factor (:352-356): the minimum over all
+ * voxels of the number of views with weight > 0, and the mean over the num_portions portions
+ * of FusionHelper.divideIntoPortions(n, num_portions) of each portion's mean count (the
+ * reference uses 2 x its thread count).  Run on the weights before normalisation (a weight's
+ * sign does not change); waits for `stream`. */
+int mvd_weight_overlap(const float* const* weights, int num_views, long long n, int num_portions, int* min_views,
+                       double* avg_views, int devCUDA, void* stream);
 
 #ifdef __cplusplus
 }

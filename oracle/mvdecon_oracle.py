@@ -530,3 +530,33 @@ def normalize_weights_virtual(weights, osem=1.0):
         s += w.astype(np.float64)
     norm = np.where(s > 1, s.astype(np.float32), np.float32(1)).astype(np.float64)
     return [np.minimum(1.0, w.astype(np.float64) / norm * osem).astype(np.float32) for w in weights]
+
+
+def normalize_weights_precomputed(weights, osem=1.0):
+    """PRECOMPUTED weights (WeightNormalizer.ApplyDirectly, WeightNormalizer.java:132-185, then
+    ProcessForDeconvolution.adjustForOSEM, :376-383): (float)(w_v / sum) with no guard on the
+    sum (NaN where every view has weight 0), then Math.min(1, w * (float)osem) in float, NaN
+    kept (Math.min propagates NaN)."""
+    s = np.zeros(weights[0].shape, dtype=np.float64)
+    for w in weights:
+        s += w.astype(np.float64)
+    out = []
+    with np.errstate(invalid="ignore", divide="ignore"):
+        for w in weights:
+            x = (w.astype(np.float64) / s).astype(np.float32)
+            y = x * np.float32(osem)
+            out.append(np.where(np.isnan(y), y, np.minimum(np.float32(1), y)).astype(np.float32))
+    return out
+
+
+def weight_overlap(weights, num_portions):
+    """WeightNormalizer's overlap statistics (WeightNormalizer.java:94-106, 187-252): the minimum
+    per-voxel count of views with weight > 0, and the mean over the portions of
+    divideIntoPortions(n, num_portions) of each portion's mean count."""
+    count = np.zeros(weights[0].size, dtype=np.int64)
+    for w in weights:
+        count += (w.ravel() > 0)
+    avg = 0.0
+    for start, loop in divide_into_portions(count.size, num_portions):
+        avg += float(count[start:start + loop].sum()) / loop
+    return int(count.min()), avg / num_portions

@@ -15,3 +15,4 @@ from .mvdecon import (  # noqa: F401
     MVDeconInput,
     MVDeconvolution,
 )
+from .inputs import WeightNormalizer, WeightType, transform_input  # noqa: F401,E402

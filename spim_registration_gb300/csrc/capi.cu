@@ -655,11 +655,13 @@ extern "C" int mvd_create(mvd_decon** out, int devCUDA, const int* dims, int num
     h->kd.push_back({psf_dims[3 * v], psf_dims[3 * v + 1], psf_dims[3 * v + 2]});
     h->img[v].alloc(nb);
     h->w[v].alloc(nb);
-    MVD_CHECK(cudaMemcpyAsync(h->img[v].p, views[v], nb, cudaMemcpyHostToDevice, h->stream));
-    MVD_CHECK(cudaMemcpyAsync(h->w[v].p, weights[v], nb, cudaMemcpyHostToDevice, h->stream));
+    // cudaMemcpyDefault: the inputs may be host memory or device memory (for example views
+    // resampled on the GPU by mvd_transform_view); unified addressing tells them apart
+    MVD_CHECK(cudaMemcpyAsync(h->img[v].p, views[v], nb, cudaMemcpyDefault, h->stream));
+    MVD_CHECK(cudaMemcpyAsync(h->w[v].p, weights[v], nb, cudaMemcpyDefault, h->stream));
     const size_t kb = vox(h->kd[v]) * sizeof(float);
     h->k1[v].alloc(kb);
-    MVD_CHECK(cudaMemcpyAsync(h->k1[v].p, psfs[v], kb, cudaMemcpyHostToDevice, h->stream));
+    MVD_CHECK(cudaMemcpyAsync(h->k1[v].p, psfs[v], kb, cudaMemcpyDefault, h->stream));
   }
   PhaseTrace trace(h->stream);
   MVD_CHECK(cudaStreamSynchronize(h->stream));

@@ -9,6 +9,7 @@
 #include <cmath>
 #include <cstring>
 #include <string>
+#include <vector>
 
 #include "../../include/mvdecon.h"
 #include "engine.h"
@@ -104,18 +105,74 @@ struct WeightPtrs {
   float* p[16];
 };
 
-// VIRTUAL: w_v / (sum_w > 1 ? sum_w : 1) (sum in double, the normaliser stored as float),
-// then min(1, w * osem)
-__global__ void normalize_weights_kernel(WeightPtrs w, int nv, long long n, double osem) {
+// mode 0, VIRTUAL (NormalizingRandomAccess.get): w_v / (sum_w > 1 ? sum_w : 1), the sum in
+// double and the normaliser stored as float, then min(1, w * osem) in double.
+// mode 1, PRECOMPUTED (WeightNormalizer.ApplyDirectly + ProcessForDeconvolution.adjustForOSEM):
+// (float)(w_v / sum_w) with no guard on the sum (0 / 0 gives NaN where no view has weight, as
+// in the reference), then min(1, w * (float)osem) in float.
+__global__ void normalize_weights_kernel(WeightPtrs w, int nv, long long n, double osem, int mode) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
     double sum = 0.0;
     for (int v = 0; v < nv; ++v) sum += (double)w.p[v][i];
-    const float norm = sum > 1.0 ? (float)sum : 1.f;
-    for (int v = 0; v < nv; ++v) {
-      const double x = (double)w.p[v][i] / (double)norm;
-      w.p[v][i] = (float)fmin(1.0, x * osem);
+    if (mode == 0) {
+      const float norm = sum > 1.0 ? (float)sum : 1.f;
+      for (int v = 0; v < nv; ++v) {
+        const double x = (double)w.p[v][i] / (double)norm;
+        w.p[v][i] = (float)fmin(1.0, x * osem);
+      }
+    } else {
+      const float fo = (float)osem;
+      for (int v = 0; v < nv; ++v) {
+        const float x = (float)((double)w.p[v][i] / sum);
+        // Math.min(1, NaN) is NaN; fminf would return 1
+        const float y = __fmul_rn(x, fo);
+        w.p[v][i] = (y != y) ? y : fminf(1.f, y);
+      }
     }
   }
+}
+
+// WeightNormalizer's overlap statistics (WeightNormalizer.java:187-252): per voxel the number
+// of views with weight > 0; the minimum over the volume and, per portion of
+// FusionHelper.divideIntoPortions(n, P), the sum of the counts.  Each block walks one
+// contiguous range, so a warp's 32 voxels lie in one portion except at the few portion
+// borders; lane 0 keeps the running sum of its portion in a register.
+__global__ void weight_overlap_kernel(WeightPtrs w, int nv, long long n, long long chunk, int portions,
+                                      long long span, unsigned long long* __restrict__ portion_sum,
+                                      int* __restrict__ min_count) {
+  const long long lo = blockIdx.x * span;
+  const long long hi = lo + span < n ? lo + span : n;
+  const int lane = threadIdx.x & 31;
+  int local_min = nv;
+  int cur = -1;
+  unsigned long long acc = 0;
+  for (long long base = lo + (threadIdx.x & ~31); base < hi; base += blockDim.x) {
+    const long long i = base + lane;
+    int c = 0;
+    if (i < hi) {
+      for (int v = 0; v < nv; ++v) c += w.p[v][i] > 0.f;
+      local_min = min(local_min, c);
+    }
+    const long long last = (base + 31 < hi ? base + 31 : hi - 1);
+    const int p0 = (int)min((long long)portions - 1, base / chunk);
+    const int p1 = (int)min((long long)portions - 1, last / chunk);
+    if (p0 == p1) {
+      const unsigned s = __reduce_add_sync(0xffffffffu, (unsigned)c);
+      if (lane == 0) {
+        if (p0 != cur) {
+          if (cur >= 0 && acc) atomicAdd(portion_sum + cur, acc);
+          cur = p0;
+          acc = 0;
+        }
+        acc += s;
+      }
+    } else if (i < hi && c) {
+      atomicAdd(portion_sum + (int)min((long long)portions - 1, i / chunk), (unsigned long long)c);
+    }
+  }
+  if (lane == 0 && cur >= 0 && acc) atomicAdd(portion_sum + cur, acc);
+  const int m = __reduce_min_sync(0xffffffffu, local_min);
+  if (lane == 0) atomicMin(min_count, m);
 }
 
 int grid_n(long long n) {
@@ -207,12 +264,12 @@ extern "C" int mvd_transform_view(const float* view, const int* vd, const double
   }
 }
 
-extern "C" int mvd_normalize_weights(float* const* weights, int num_views, long long n, double osem, int devCUDA,
-                                     void* stream) {
+extern "C" int mvd_normalize_weights(float* const* weights, int num_views, long long n, double osem, int mode,
+                                     int devCUDA, void* stream) {
   try {
     set_last_error("");
-    if (!weights || num_views < 1 || num_views > 16 || n < 0) {
-      set_last_error("bad arguments (1..16 weight volumes)");
+    if (!weights || num_views < 1 || num_views > 16 || n < 0 || (mode != 0 && mode != 1)) {
+      set_last_error("bad arguments (1..16 weight volumes, mode 0 or 1)");
       return MVD_ERR_ARG;
     }
     WeightPtrs wp{};
@@ -225,9 +282,66 @@ extern "C" int mvd_normalize_weights(float* const* weights, int num_views, long 
     }
     MVD_CHECK(cudaSetDevice(devCUDA));
     if (n == 0) return MVD_OK;
-    normalize_weights_kernel<<<grid_n(n), 256, 0, static_cast<cudaStream_t>(stream)>>>(wp, num_views, n, osem);
+    normalize_weights_kernel<<<grid_n(n), 256, 0, static_cast<cudaStream_t>(stream)>>>(wp, num_views, n, osem, mode);
     MVD_CHECK(cudaGetLastError());
     count_launch();
+    return MVD_OK;
+  } catch (const CudaError& e) {
+    set_last_error(e.what());
+    return MVD_ERR_CUDA;
+  } catch (const std::exception& e) {
+    set_last_error(e.what());
+    return MVD_ERR_INTERNAL;
+  }
+}
+
+extern "C" int mvd_weight_overlap(const float* const* weights, int num_views, long long n, int num_portions,
+                                  int* min_views, double* avg_views, int devCUDA, void* stream) {
+  try {
+    set_last_error("");
+    if (!weights || num_views < 1 || num_views > 16 || n < 1 || num_portions < 1 || num_portions > 65536 ||
+        (long long)num_portions > n || !min_views || !avg_views) {
+      set_last_error("bad arguments (1..16 weight volumes, 1 <= num_portions <= min(n, 65536))");
+      return MVD_ERR_ARG;
+    }
+    WeightPtrs wp{};
+    for (int v = 0; v < num_views; ++v) {
+      if (!weights[v]) {
+        set_last_error("NULL weight volume");
+        return MVD_ERR_ARG;
+      }
+      wp.p[v] = const_cast<float*>(weights[v]);
+    }
+    MVD_CHECK(cudaSetDevice(devCUDA));
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    // device scratch: the portion sums, then the minimum
+    const size_t bytes = (size_t)num_portions * sizeof(unsigned long long) + sizeof(int);
+    DevBuf scratch;
+    scratch.alloc(bytes);
+    unsigned long long* d_sum = scratch.as<unsigned long long>();
+    int* d_min = reinterpret_cast<int*>(d_sum + num_portions);
+    MVD_CHECK(cudaMemsetAsync(d_sum, 0, (size_t)num_portions * sizeof(unsigned long long), s));
+    MVD_CHECK(cudaMemcpyAsync(d_min, &num_views, sizeof(int), cudaMemcpyHostToDevice, s));
+    const int grid = grid_n(n);
+    long long span = (n + grid - 1) / grid;
+    span = (span + 31) / 32 * 32;
+    const long long chunk = n / num_portions;
+    weight_overlap_kernel<<<grid, 256, 0, s>>>(wp, num_views, n, chunk, num_portions, span, d_sum, d_min);
+    MVD_CHECK(cudaGetLastError());
+    count_launch();
+    std::vector<unsigned long long> sums(num_portions);
+    int mn = 0;
+    MVD_CHECK(cudaMemcpyAsync(sums.data(), d_sum, sums.size() * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+    MVD_CHECK(cudaMemcpyAsync(&mn, d_min, sizeof(int), cudaMemcpyDeviceToHost, s));
+    MVD_CHECK(cudaStreamSynchronize(s));
+    // the reference averages the per-portion averages (WeightNormalizer.java:98-106)
+    double avg = 0.0;
+    for (int p = 0; p < num_portions; ++p) {
+      const long long loop = p == num_portions - 1 ? chunk + n % num_portions : chunk;
+      avg += (double)sums[p] / (double)loop;
+    }
+    *min_views = mn;
+    *avg_views = avg / num_portions;
     return MVD_OK;
   } catch (const CudaError& e) {
     set_last_error(e.what());

@@ -125,27 +125,49 @@ class MVDeconInput:
         return len(self.views)
 
 
+def _input_array(a):
+    """A view or weight volume: a numpy array (host) or a contiguous float32 CUDA tensor (device,
+    e.g. from ``inputs.transform_input``), which mvd_create copies without a host round trip."""
+    if getattr(a, "is_cuda", False):
+        if str(a.dtype) != "torch.float32" or not a.is_contiguous():
+            raise ValueError("device volumes must be contiguous float32 tensors")
+        return a
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+def _input_ptr(a):
+    if isinstance(a, np.ndarray):
+        return native.fptr(a)
+    return ctypes.cast(ctypes.c_void_p(a.data_ptr()), native._F)
+
+
 class Deconvolution:
-    """Handle over the library's whole-deconvolution API (mvd_create / mvd_run_* / mvd_get_psi)."""
+    """Handle over the library's whole-deconvolution API (mvd_create / mvd_run_* / mvd_get_psi).
+
+    views and weights are numpy arrays or float32 CUDA tensors on ``device`` ([z, y, x])."""
 
     def __init__(self, views, weights, psfs, psftype: int, lam: float, device: int = 0, flags: int = 0,
                  block=None):
         self.lib = native.load()
-        views = [np.ascontiguousarray(v, dtype=np.float32) for v in views]
-        weights = [np.ascontiguousarray(w, dtype=np.float32) for w in weights]
+        views = [_input_array(v) for v in views]
+        weights = [_input_array(w) for w in weights]
         psfs = [np.ascontiguousarray(p, dtype=np.float32) for p in psfs]
         if not views:
             raise ValueError("no views")
-        shape = views[0].shape
+        shape = tuple(views[0].shape)
         for a in views + weights:
-            if a.shape != shape:
+            if tuple(a.shape) != shape:
                 raise ValueError("all views and weights must share one shape")
         self.shape = shape
         self.n_views = len(views)
         self._keep = (views, weights, psfs)
+        if any(not isinstance(a, np.ndarray) for a in views + weights):
+            import torch  # device inputs: the work that wrote them must be complete
+
+            torch.cuda.synchronize(device)
         nz, ny, nx = shape
-        vp = (native._F * self.n_views)(*[native.fptr(v) for v in views])
-        wp = (native._F * self.n_views)(*[native.fptr(w) for w in weights])
+        vp = (native._F * self.n_views)(*[_input_ptr(v) for v in views])
+        wp = (native._F * self.n_views)(*[_input_ptr(w) for w in weights])
         pp = (native._F * self.n_views)(*[native.fptr(p) for p in psfs])
         pd = []
         for p in psfs:

@@ -76,7 +76,9 @@ SIGNATURES = {
     "mvd_transform_view": (ctypes.c_int, [ctypes.c_void_p, _I, _D, _I, _I, ctypes.c_void_p, ctypes.c_void_p, _F, _F,
                                           ctypes.c_int, ctypes.c_void_p]),
     "mvd_normalize_weights": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int, ctypes.c_longlong,
-                                             ctypes.c_double, ctypes.c_int, ctypes.c_void_p]),
+                                             ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_void_p]),
+    "mvd_weight_overlap": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int, ctypes.c_longlong, ctypes.c_int,
+                                          _I, ctypes.POINTER(ctypes.c_double), ctypes.c_int, ctypes.c_void_p]),
 }
 
 

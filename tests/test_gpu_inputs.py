@@ -72,10 +72,93 @@ def test_normalize_weights_matches_oracle(osem):
     want = O.normalize_weights_virtual(ws, osem)
     dws = [torch.from_numpy(w).cuda() for w in ws]
     ptrs = (native.ctypes.c_void_p * 3)(*[d.data_ptr() for d in dws])
-    native.check(lib.mvd_normalize_weights(ptrs, 3, ws[0].size, osem, 0, None))
+    native.check(lib.mvd_normalize_weights(ptrs, 3, ws[0].size, osem, 0, 0, None))
     torch.cuda.synchronize()
     for d, w in zip(dws, want):
         np.testing.assert_allclose(d.cpu().numpy(), w, rtol=2e-7, atol=0)
+
+
+@pytest.mark.parametrize("osem", [1.0, 2.5])
+def test_precomputed_normalisation_matches_oracle_nan_included(osem):
+    torch = pytest.importorskip("torch")
+    lib = native.load()
+    rng = np.random.default_rng(6)
+    ws = [np.where(rng.random((20, 16, 12)) < 0.4, 0, rng.random((20, 16, 12))).astype(np.float32) for _ in range(3)]
+    want = O.normalize_weights_precomputed(ws, osem)
+    assert np.isnan(want[0]).any()
+    dws = [torch.from_numpy(w).cuda() for w in ws]
+    ptrs = (native.ctypes.c_void_p * 3)(*[d.data_ptr() for d in dws])
+    native.check(lib.mvd_normalize_weights(ptrs, 3, ws[0].size, osem, 1, 0, None))
+    torch.cuda.synchronize()
+    for d, w in zip(dws, want):
+        np.testing.assert_array_equal(d.cpu().numpy(), w)  # NaN positions included
+
+
+@pytest.mark.parametrize("portions", [1, 7, 32])
+def test_weight_overlap_matches_oracle(portions):
+    torch = pytest.importorskip("torch")
+    from spim_registration_gb300 import WeightNormalizer
+
+    rng = np.random.default_rng(7)
+    shape = (37, 29, 23)  # odd sizes: portion borders fall inside warps
+    ws = [np.where(rng.random(shape) < 0.3, 0, rng.random(shape)).astype(np.float32) for _ in range(4)]
+    mn, avg = O.weight_overlap(ws, portions)
+    wn = WeightNormalizer([torch.from_numpy(w).cuda() for w in ws], num_portions=portions)
+    assert wn.process()
+    assert wn.getMinOverlappingViews() == mn
+    assert wn.getAvgOverlappingViews() == pytest.approx(avg, rel=1e-12)
+    ws[1][:] = 0.5  # every voxel covered at least once
+    wn = WeightNormalizer([torch.from_numpy(w).cuda() for w in ws], num_portions=portions)
+    wn.process()
+    assert wn.getMinOverlappingViews() == O.weight_overlap(ws, portions)[0] >= 1
+
+
+def test_raw_views_to_deconvolution_on_the_device():
+    """Raw views + registrations -> resampled views and blending weights -> overlap statistics
+    -> VIRTUAL normalisation with the average-overlap OSEM factor -> deconvolution from the
+    device tensors; the oracle runs the same chain in FP64."""
+    torch = pytest.importorskip("torch")
+    from spim_registration_gb300 import PSFTYPE, Deconvolution, WeightNormalizer, transform_input
+    from spim_registration_gb300 import synthetic as S
+    from tests.helpers import rel_l2
+
+    rng = np.random.default_rng(8)
+    box = (36, 40, 44)  # z, y, x
+    offset = (-3, -2, -4)
+    raw, affines = [], []
+    for angle in (0.0, 40.0, 90.0):
+        raw.append((S.gaussian_psf((3.0, 3.0, 3.0), (41, 37, 33), 0.0) * 5000 + rng.random((33, 37, 41)) * 10
+                    + 1).astype(np.float32))
+        c, s_ = math.cos(math.radians(angle)), math.sin(math.radians(angle))
+        # the view centre (20, 18, 16 * 1.25) lands near the box centre (18, 18, 15), off the grid
+        shift = (18.25 - (20 * c + 20 * s_), 0.375, 15.125 - (-20 * s_ + 20 * c))
+        affines.append(_affine(angle, (1.0, 1.0, 1.25), shift))
+    border, blend = (0.0, 0.0, 0.0), (8.0, 8.0, 6.0)
+    psfs = [(lambda k: (k / k.sum()).astype(np.float32))(S.gaussian_psf((1.2, 1.2, 2.5), (7, 7, 11), 0.0))
+            for _ in raw]
+    dev_views, dev_weights = [], []
+    for r, a in zip(raw, affines):
+        img, w = transform_input(r, a, offset, box, border, blend)
+        dev_views.append(img)
+        dev_weights.append(w)
+    wn = WeightNormalizer(dev_weights, num_portions=8)
+    wn.process()
+    osem = wn.osem_speedup(2)
+    wn.apply(osem)
+    d = Deconvolution(dev_views, dev_weights, psfs, PSFTYPE.EFFICIENT_BAYESIAN, 0.006)
+    d.run(3)
+    got = d.get_psi()
+
+    views = [O.transform_input(r, a, offset, box).astype(np.float32) for r, a in zip(raw, affines)]
+    weights = [O.transform_weights(r.shape, a, offset, box, border, blend) for r, a in zip(raw, affines)]
+    mn, avg = O.weight_overlap(weights, 8)
+    assert wn.getMinOverlappingViews() == mn and osem == pytest.approx(max(1.0, avg), rel=1e-12)
+    weights = O.normalize_weights_virtual(weights, max(1.0, avg))
+    for dv, v in zip(dev_views, views):
+        assert rel_l2(dv.cpu().numpy(), v) < 1e-5
+    p = S.Problem("raw", views, weights, psfs, int(PSFTYPE.EFFICIENT_BAYESIAN), 3, 0.006, None)
+    ref, _ = O.deconvolve(p, arith="f64", block=None, mask=False)
+    assert rel_l2(got, ref) < 1e-4, rel_l2(got, ref)
 
 
 def test_transform_view_rejects_singular_affines():

@@ -219,3 +219,22 @@ def test_virtual_weight_normalisation():
     np.testing.assert_allclose(n1[0][~big], ws[0][~big], rtol=1e-7)
     n2 = O.normalize_weights_virtual(ws, 3.0)
     assert np.all(n2[0] <= 1) and np.all(n2[0] >= np.minimum(1, n1[0] * 3 * (1 - 1e-6)))
+
+
+def test_precomputed_weight_normalisation_and_overlap():
+    rng = np.random.default_rng(13)
+    ws = [np.where(rng.random((4, 5, 6)) < 0.3, 0, rng.random((4, 5, 6))).astype(np.float32) for _ in range(3)]
+    ws[0][0, 0, 0] = ws[1][0, 0, 0] = ws[2][0, 0, 0] = 0  # no view: 0 / 0
+    n = O.normalize_weights_precomputed(ws, 1.0)
+    s = np.sum(n, axis=0)
+    covered = np.sum(ws, axis=0) > 0
+    assert np.all(np.isnan(s[~covered])) and not covered[0, 0, 0]
+    np.testing.assert_allclose(s[covered], 1, rtol=1e-6)  # no guard: sums below 1 are raised too
+    n2 = O.normalize_weights_precomputed(ws, 2.5)
+    assert np.isnan(n2[0][0, 0, 0]) and np.nanmax(n2[0]) <= 1
+    mn, avg = O.weight_overlap(ws, 7)
+    cnt = sum((w > 0).astype(int) for w in ws).ravel()
+    assert mn == 0
+    # equal portions except the last one: the mean of portion means differs from the plain mean
+    portions = O.divide_into_portions(cnt.size, 7)
+    assert avg == pytest.approx(np.mean([cnt[s:s + l].mean() for s, l in portions]), rel=1e-12)
