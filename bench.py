@@ -309,6 +309,8 @@ def run_ours(args, rank, world, local):
 
     if rank == 0 and not args.no_e2e:
         out["e2e"] = run_e2e(prob, local, steps=2)
+    if rank == 0:
+        out["input_preparation"] = run_inputs(prob, local, hbm_peak)
     if rank == 0 and not args.no_cpu:
         out["cpu_baseline"] = cpu_baseline(prob)
     return out
@@ -347,6 +349,58 @@ def run_e2e(prob, device, steps=2):
     return {"value": prob.n_voxels * len(prob.views) * prob.iterations / t, "unit": "voxel-updates/s",
             "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "seconds_per_job": t,
             "step": f"one whole job: upload + kernel prep + {prob.iterations} iterations + masked psi download"}
+
+
+def run_inputs(prob, device, hbm_peak, reps=5):
+    """Input preparation on the device at the workload's size: every view (raw stack of the
+    fused box's size, rotated about y by 180 v / V degrees with a fractional shift) resampled
+    with its blending weight, the overlap statistics and the VIRTUAL normalisation with the
+    average-overlap OSEM factor.  Algorithmic bytes: resample 4 (view) + 8 (image, weight)
+    per voxel and view; overlap 4 per voxel and view; normalisation 8 per voxel and view."""
+    import math
+
+    import torch
+
+    from spim_registration_gb300 import WeightNormalizer, transform_input
+
+    nz, ny, nx = prob.views[0].shape
+    V = len(prob.views)
+    n = nx * ny * nz
+    raw = [torch.from_numpy(np.ascontiguousarray(v)).to(f"cuda:{device}") for v in prob.views]
+    cx, cy, cz = (nx - 1) / 2, (ny - 1) / 2, (nz - 1) / 2
+    affines = []
+    for v in range(V):
+        t = math.radians(180.0 * v / V)
+        c, s_ = math.cos(t), math.sin(t)
+        shift = (cx - (c * cx + s_ * cz) + 0.25, 0.375, cz - (-s_ * cx + c * cz) + 0.125)
+        affines.append([c, 0, s_, shift[0], 0, 1, 0, shift[1], -s_, 0, c, shift[2]])
+    border, blend = (0.0, 0.0, 0.0), (20.0, 20.0, 20.0)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    ms = np.zeros(3)
+    for r in range(reps + 1):
+        torch.cuda.synchronize()
+        ev[0].record()
+        outs = [transform_input(raw[v], affines[v], (0, 0, 0), (nz, ny, nx), border, blend, device) for v in range(V)]
+        ev[1].record()
+        wn = WeightNormalizer([o[1] for o in outs], num_portions=32)
+        wn.process()  # waits for the stream: returns the statistics to the host
+        ev[2].record()
+        wn.apply(wn.osem_speedup(2))
+        ev[3].record()
+        torch.cuda.synchronize()
+        if r:
+            ms += [ev[0].elapsed_time(ev[1]), ev[1].elapsed_time(ev[2]), ev[2].elapsed_time(ev[3])]
+        del outs, wn
+    ms /= reps
+    algo = [12.0 * n * V, 4.0 * n * V, 8.0 * n * V]
+    names = ["transform_view", "weight_overlap", "normalize_weights"]
+    res = {k: {"ms": round(float(t), 4), "gbs": round(b / (t / 1e3) / 1e9, 1),
+               "frac_of_measured_hbm": round(b / (t / 1e3) / 1e9 / hbm_peak, 3)} for k, t, b in zip(names, ms, algo)}
+    res["views"] = V
+    res["box_xyz"] = [nx, ny, nz]
+    res["total_ms"] = round(float(ms.sum()), 4)
+    res["note"] = "weight_overlap includes its device-to-host read of the statistics"
+    return res
 
 
 def cpu_view_stage_time(prob, workers=None):

@@ -188,7 +188,9 @@ int mvd_transform_view(const float* view, const int* view_dims_xyz, const double
  * volumes of n voxels (WeightNormalizer.java:73-253, ProcessForDeconvolution.java:372-405).
  * mode 0, VIRTUAL (NormalizingRandomAccess.java:57-66): w_v / (sum_w > 1 ? sum_w : 1), then
  * min(1, w * osem).  mode 1, PRECOMPUTED (WeightNormalizer.ApplyDirectly): w_v / sum_w, then
- * min(1, w * (float)osem); NaN where no view has weight, as in the reference. */
+ * min(1, w * (float)osem); NaN where no view has weight, as in the reference.  Results equal
+ * the reference's double arithmetic bit for bit (certified float-pair arithmetic, with the rare
+ * undecided voxels finished in double).  Allocates a stream-ordered scratch list. */
 int mvd_normalize_weights(float* const* weights, int num_views, long long n, double osem, int mode, int devCUDA,
                           void* stream);
 /* WeightNormalizer's overlap statistics (WeightNormalizer.java:94-106, 187-252), which

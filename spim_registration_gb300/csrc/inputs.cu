@@ -80,56 +80,184 @@ __device__ __forceinline__ float blend_weight(float lx, float ly, float lz, int 
   return w;
 }
 
-__global__ void transform_view_kernel(const float* __restrict__ view, int sx, int sy, int sz, Affine inv, int ox,
-                                      int oy, int oz, int nx, int ny, int nz, float* __restrict__ out_img,
-                                      float* __restrict__ out_blend, float3 border, float3 range) {
-  const long long n = (long long)nx * ny * nz;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-    const int x = (int)(i % nx), y = (int)((i / nx) % ny), z = (int)(i / ((long long)nx * ny));
-    const float s0 = (float)(x + ox), s1 = (float)(y + oy), s2 = (float)(z + oz);
-    const float t0 = inv.m[0] * s0 + inv.m[1] * s1 + inv.m[2] * s2 + inv.m[3];
-    const float t1 = inv.m[4] * s0 + inv.m[5] * s1 + inv.m[6] * s2 + inv.m[7];
-    const float t2 = inv.m[8] * s0 + inv.m[9] * s1 + inv.m[10] * s2 + inv.m[11];
-    if (out_img) {
-      float v = 0.f;  // no image data (MVDeconvolution.computeQuotient reads 0 as "no data")
-      if (t0 >= 0.f && t1 >= 0.f && t2 >= 0.f && t0 < (float)sx && t1 < (float)sy && t2 < (float)sz)
-        v = fmaxf(1e-4f, trilinear_mirror(view, sx, sy, sz, t0, t1, t2));
-      out_img[i] = v;
-    }
-    // the blending weight is defined everywhere (the border can be negative)
-    if (out_blend) out_blend[i] = blend_weight(t0, t1, t2, sx, sy, sz, border, range);
+// One thread per output voxel; a block covers a 32 x 8 patch of one z plane, so its view
+// positions stay close together whatever the rotation (the view's reads hit L1/L2).
+__global__ void __launch_bounds__(256) transform_view_kernel(const float* __restrict__ view, int sx, int sy, int sz,
+                                                             Affine inv, int ox, int oy, int oz, int nx, int ny,
+                                                             float* __restrict__ out_img,
+                                                             float* __restrict__ out_blend, float3 border,
+                                                             float3 range) {
+  const int x = blockIdx.x * 32 + threadIdx.x, y = blockIdx.y * 8 + threadIdx.y, z = blockIdx.z;
+  if (x >= nx || y >= ny) return;
+  const long long i = ((long long)z * ny + y) * nx + x;
+  const float s0 = (float)(x + ox), s1 = (float)(y + oy), s2 = (float)(z + oz);
+  const float t0 = inv.m[0] * s0 + inv.m[1] * s1 + inv.m[2] * s2 + inv.m[3];
+  const float t1 = inv.m[4] * s0 + inv.m[5] * s1 + inv.m[6] * s2 + inv.m[7];
+  const float t2 = inv.m[8] * s0 + inv.m[9] * s1 + inv.m[10] * s2 + inv.m[11];
+  if (out_img) {
+    float v = 0.f;  // no image data (MVDeconvolution.computeQuotient reads 0 as "no data")
+    if (t0 >= 0.f && t1 >= 0.f && t2 >= 0.f && t0 < (float)sx && t1 < (float)sy && t2 < (float)sz)
+      v = fmaxf(1e-4f, trilinear_mirror(view, sx, sy, sz, t0, t1, t2));
+    out_img[i] = v;
   }
+  // the blending weight is defined everywhere (the border can be negative)
+  if (out_blend) out_blend[i] = blend_weight(t0, t1, t2, sx, sy, sz, border, range);
 }
 
 struct WeightPtrs {
   float* p[16];
 };
 
+// Math.min(1, x) of the reference: NaN stays NaN (fminf would return 1)
+__device__ __forceinline__ float java_min1(float x) { return x != x ? x : fminf(1.f, x); }
+
+// The reference normalises in double; GB300's FP64 pipe is a small fraction of its FP32 one.
+// The sum over the views stays in double (the reference's sequential double sum cannot be
+// reproduced otherwise), but the per-view quotients and OSEM products are carried as
+// unevaluated float pairs (hi + lo, within ~2^-44 relative of the exact value) built from
+// error-free transformations, rounded once at the end.  Each rounding is certified: when the
+// pair lies within 2^-14 of a half ulp from a rounding boundary (or the result is a power of
+// two or denormal), only the reference's double rounding decides it.  Such voxels are left
+// unwritten and appended to a list (warp-aggregated atomics), which a second kernel finishes
+// with the reference's double arithmetic, so no warp diverges into the double path.  They are
+// rare for a generic OSEM factor (~1e-4) but common for decimal ones: w * 1.7 is an exact tie
+// in rational arithmetic for ~5% of floats w, and the double 1.7 sits just beside it.
+
+struct FF {  // hi + lo
+  float hi, lo;
+};
+
+// y = the float nearest hi + lo; false when that rounding is not certain
+__device__ __forceinline__ bool round_pair(FF x, float& y) {
+  y = __fadd_rn(x.hi, x.lo);
+  if (x.lo == 0.f) return true;
+  const unsigned b = __float_as_uint(y);
+  const unsigned ex = b & 0x7f800000u;
+  if (ex <= (24u << 23) || ex == 0x7f800000u || (b & 0x007fffffu) == 0u) return false;
+  const float half_ulp = __uint_as_float(ex - (24u << 23));
+  const float d = __fadd_rn(__fsub_rn(x.hi, y), x.lo);  // (hi + lo) - y; hi - y is exact
+  return fabsf(d) < __fmul_rn(half_ulp, 0.99993896484375f);
+}
+
+// w / (d.hi + d.lo) as a pair: q = fl(w / d.hi) is correctly rounded, so w - q d.hi is exact
+// (an FMA); the remainder over d gives the low part.
+__device__ __forceinline__ FF ff_quotient(float w, FF d) {
+  const float q = __fdiv_rn(w, d.hi);
+  const float r = __fsub_rn(__fmaf_rn(-q, d.hi, w), __fmul_rn(q, d.lo));
+  return {q, __fmul_rn(r, __frcp_rn(d.hi))};
+}
+
+// (a.hi + a.lo) * (b.hi + b.lo) as a pair
+__device__ __forceinline__ FF ff_mul(FF a, FF b) {
+  const float p = __fmul_rn(a.hi, b.hi);
+  const float e = __fmaf_rn(a.hi, b.hi, -p);
+  return {p, __fadd_rn(e, __fadd_rn(__fmul_rn(a.hi, b.lo), __fmul_rn(a.lo, b.hi)))};
+}
+
+// One voxel with the reference's own double arithmetic; the weights are read again from
+// memory, which the certified pass has not written for this voxel.
+__device__ __forceinline__ void normalize_voxel_double(const WeightPtrs& w, int nv, long long i, double osem,
+                                                       int mode) {
+  double sum = 0.0;
+#pragma unroll
+  for (int v = 0; v < 16; ++v)
+    if (v < nv) sum += (double)w.p[v][i];
+  const float norm = sum > 1.0 ? (float)sum : 1.f;
+#pragma unroll
+  for (int v = 0; v < 16; ++v)
+    if (v < nv) {
+      const float wv = w.p[v][i];
+      if (mode == 0) {
+        const double x = (double)wv / (double)norm * osem;
+        w.p[v][i] = (float)(x != x ? x : fmin(1.0, x));
+      } else {
+        w.p[v][i] = java_min1(__fmul_rn((float)((double)wv / sum), (float)osem));
+      }
+    }
+}
+
+struct Deferred {  // voxels left to the double pass
+  long long* list;
+  unsigned long long* count;
+  unsigned long long cap;
+};
+
 // mode 0, VIRTUAL (NormalizingRandomAccess.get): w_v / (sum_w > 1 ? sum_w : 1), the sum in
-// double and the normaliser stored as float, then min(1, w * osem) in double.
+// double and the normaliser stored as float, then min(1, w * osem) in double.  For osem == 1
+// the float division is the result: the double quotient of two floats rounded to float is the
+// correctly rounded float quotient.
 // mode 1, PRECOMPUTED (WeightNormalizer.ApplyDirectly + ProcessForDeconvolution.adjustForOSEM):
 // (float)(w_v / sum_w) with no guard on the sum (0 / 0 gives NaN where no view has weight, as
 // in the reference), then min(1, w * (float)osem) in float.
-__global__ void normalize_weights_kernel(WeightPtrs w, int nv, long long n, double osem, int mode) {
+// osem arrives as a float pair too (osem_hi + osem_lo == osem to ~48 bits).
+__global__ void normalize_weights_kernel(WeightPtrs w, int nv, long long n, double osem, float osem_hi,
+                                         float osem_lo, int mode, Deferred def) {
+  const FF os = {osem_hi, osem_lo};
+  const bool unit = osem == 1.0;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-    double sum = 0.0;
-    for (int v = 0; v < nv; ++v) sum += (double)w.p[v][i];
+    float wv[16], out[16];
+#pragma unroll
+    for (int v = 0; v < 16; ++v)
+      if (v < nv) wv[v] = w.p[v][i];
+    double sum_d = 0.0;
+#pragma unroll
+    for (int v = 0; v < 16; ++v)
+      if (v < nv) sum_d += (double)wv[v];
+    bool certain = true;
     if (mode == 0) {
-      const float norm = sum > 1.0 ? (float)sum : 1.f;
-      for (int v = 0; v < nv; ++v) {
-        const double x = (double)w.p[v][i] / (double)norm;
-        w.p[v][i] = (float)fmin(1.0, x * osem);
-      }
+      const float norm = sum_d > 1.0 ? (float)sum_d : 1.f;
+#pragma unroll
+      for (int v = 0; v < 16; ++v)
+        if (v < nv) {
+          float y;
+          if (unit) {
+            y = __fdiv_rn(wv[v], norm);
+          } else {
+            certain = round_pair(ff_mul(ff_quotient(wv[v], FF{norm, 0.f}), os), y) && certain;
+          }
+          out[v] = java_min1(y);
+        }
     } else {
-      const float fo = (float)osem;
-      for (int v = 0; v < nv; ++v) {
-        const float x = (float)((double)w.p[v][i] / sum);
-        // Math.min(1, NaN) is NaN; fminf would return 1
-        const float y = __fmul_rn(x, fo);
-        w.p[v][i] = (y != y) ? y : fminf(1.f, y);
-      }
+      const float s_hi = (float)sum_d;
+      const FF sum = {s_hi, (float)(sum_d - (double)s_hi)};
+#pragma unroll
+      for (int v = 0; v < 16; ++v)
+        if (v < nv) {
+          float x = 0.f;
+          if (sum_d == 0.0) {
+            x = __fdiv_rn(wv[v], 0.f);  // w / 0: NaN (0 / 0) or an infinity, as in double
+          } else {
+            certain = round_pair(ff_quotient(wv[v], sum), x) && certain;
+          }
+          out[v] = java_min1(__fmul_rn(x, osem_hi));  // (float)osemspeedup: the float osem
+        }
+    }
+    if (certain) {
+#pragma unroll
+      for (int v = 0; v < 16; ++v)
+        if (v < nv) w.p[v][i] = out[v];
+    } else {
+      const unsigned m = __activemask();  // the lanes deferring a voxel in this step
+      const int lane = threadIdx.x & 31;
+      const int leader = __ffs(m) - 1;
+      unsigned long long base = 0;
+      if (lane == leader) base = atomicAdd(def.count, (unsigned long long)__popc(m));
+      base = __shfl_sync(m, base, leader);
+      const unsigned long long slot = base + __popc(m & ((1u << lane) - 1u));
+      if (slot < def.cap)
+        def.list[slot] = i;
+      else
+        normalize_voxel_double(w, nv, i, osem, mode);  // list full: finish it here
     }
   }
+}
+
+__global__ void normalize_deferred_kernel(WeightPtrs w, int nv, double osem, int mode, Deferred def) {
+  const unsigned long long cnt = *def.count;
+  const unsigned long long m = cnt < def.cap ? cnt : def.cap;
+  for (unsigned long long j = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; j < m;
+       j += (unsigned long long)gridDim.x * blockDim.x)
+    normalize_voxel_double(w, nv, def.list[j], osem, mode);
 }
 
 // WeightNormalizer's overlap statistics (WeightNormalizer.java:187-252): per voxel the number
@@ -150,7 +278,9 @@ __global__ void weight_overlap_kernel(WeightPtrs w, int nv, long long n, long lo
     const long long i = base + lane;
     int c = 0;
     if (i < hi) {
-      for (int v = 0; v < nv; ++v) c += w.p[v][i] > 0.f;
+#pragma unroll
+      for (int v = 0; v < 16; ++v)
+        if (v < nv) c += w.p[v][i] > 0.f;
       local_min = min(local_min, c);
     }
     const long long last = (base + 31 < hi ? base + 31 : hi - 1);
@@ -247,11 +377,15 @@ extern "C" int mvd_transform_view(const float* view, const int* vd, const double
     }
     MVD_CHECK(cudaSetDevice(devCUDA));
     upload_lut(devCUDA);
-    const long long n = (long long)od[0] * od[1] * od[2];
     const float3 b = out_blend ? make_float3(border[0], border[1], border[2]) : make_float3(0.f, 0.f, 0.f);
     const float3 r = out_blend ? make_float3(blending[0], blending[1], blending[2]) : make_float3(1.f, 1.f, 1.f);
-    transform_view_kernel<<<grid_n(n), 256, 0, static_cast<cudaStream_t>(stream)>>>(
-        view, vd[0], vd[1], vd[2], inv, offset[0], offset[1], offset[2], od[0], od[1], od[2], out_img, out_blend, b, r);
+    if (od[2] > 65535 || od[1] > 8 * 65535) {
+      set_last_error("output height above 524280 or depth above 65535");
+      return MVD_ERR_ARG;
+    }
+    const dim3 grid((od[0] + 31) / 32, (od[1] + 7) / 8, od[2]);
+    transform_view_kernel<<<grid, dim3(32, 8), 0, static_cast<cudaStream_t>(stream)>>>(
+        view, vd[0], vd[1], vd[2], inv, offset[0], offset[1], offset[2], od[0], od[1], out_img, out_blend, b, r);
     MVD_CHECK(cudaGetLastError());
     count_launch();
     return MVD_OK;
@@ -282,9 +416,24 @@ extern "C" int mvd_normalize_weights(float* const* weights, int num_views, long 
     }
     MVD_CHECK(cudaSetDevice(devCUDA));
     if (n == 0) return MVD_OK;
-    normalize_weights_kernel<<<grid_n(n), 256, 0, static_cast<cudaStream_t>(stream)>>>(wp, num_views, n, osem, mode);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const float osem_hi = (float)osem;
+    const float osem_lo = (float)(osem - (double)osem_hi);
+    // the deferred-voxel list, stream-ordered so that the call stays asynchronous
+    Deferred def;
+    def.cap = (unsigned long long)(n < (1LL << 22) ? n : (1LL << 22));
+    void* buf = nullptr;
+    MVD_CHECK(cudaMallocAsync(&buf, sizeof(unsigned long long) + def.cap * sizeof(long long), s));
+    def.count = static_cast<unsigned long long*>(buf);
+    def.list = reinterpret_cast<long long*>(def.count + 1);
+    MVD_CHECK(cudaMemsetAsync(def.count, 0, sizeof(unsigned long long), s));
+    normalize_weights_kernel<<<grid_n(n), 256, 0, s>>>(wp, num_views, n, osem, osem_hi, osem_lo, mode, def);
     MVD_CHECK(cudaGetLastError());
     count_launch();
+    normalize_deferred_kernel<<<152 * 4, 256, 0, s>>>(wp, num_views, osem, mode, def);
+    MVD_CHECK(cudaGetLastError());
+    count_launch();
+    MVD_CHECK(cudaFreeAsync(buf, s));
     return MVD_OK;
   } catch (const CudaError& e) {
     set_last_error(e.what());
