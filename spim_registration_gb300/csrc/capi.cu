@@ -552,8 +552,10 @@ void prepare_kernels(mvd_decon* h) {
 // A view's convolutions only need to cover the bounding box of its data or weight (img > 0
 // or w > 0): outside it the quotient is 1 (MVDeconvolution.java:519-522) and the update leaves
 // psi unchanged (weight 0, :723).  The boxes come from dev_data_box in mvd_create.
-// Tile plan of a view over its data box; with `autotune` the plane budgets below are all
-// tried and the fastest plan (one timed view stage each) is kept.
+// Tile plan of a view over its data box; with `autotune` the plane budgets below, each with
+// 384- and 256-thread plane CTAs, are all tried and the fastest plan (one timed view stage
+// each) is kept.  More warps hide more latency; fewer threads leave fewer idle at the stages'
+// last butterfly round, which wins for some plane shapes.
 std::unique_ptr<ConvPlan> plan_view(mvd_decon* h, int v, const int lo[3], const int hi[3], bool autotune) {
   const auto& k = h->kd[v];
   const int n[3] = {hi[0] - lo[0], hi[1] - lo[1], hi[2] - lo[2]};
@@ -581,20 +583,30 @@ std::unique_ptr<ConvPlan> plan_view(mvd_decon* h, int v, const int lo[3], const 
     MVD_CHECK(cudaEventCreate(&e0));
     MVD_CHECK(cudaEventCreate(&e1));
     float ms = 1e30f;
-    for (int rep = 0; rep < 4; ++rep) {  // rep 0 warms up
-      MVD_CHECK(cudaEventRecord(e0, h->stream));
-      launch_fwd_mirror(h->pt, *p, h->psi.as<float>(), spec.as<float2>(), h->stream);
-      launch_z(h->pt, *p, spec.as<float2>(), otf.as<float2>(), h->stream);
-      launch_inv_quotient(h->pt, *p, spec.as<float2>(), h->img[v].as<float>(), h->q.as<float>(), h->stream);
-      launch_fwd_value(h->pt, *p, h->q.as<float>(), 1.f, spec.as<float2>(), h->stream);
-      launch_z(h->pt, *p, spec.as<float2>(), otf.as<float2>(), h->stream);
-      launch_inv_quotient(h->pt, *p, spec.as<float2>(), h->img[v].as<float>(), h->q.as<float>(), h->stream);
-      MVD_CHECK(cudaEventRecord(e1, h->stream));
-      MVD_CHECK(cudaEventSynchronize(e1));
-      float t = 0.f;
-      MVD_CHECK(cudaEventElapsedTime(&t, e0, e1));
-      if (rep > 0) ms = std::min(ms, t);
+    int best_threads = kThreads;
+    for (int threads : {kThreads, 256}) {
+      p->threads_plane = threads;
+      float ms_t = 1e30f;
+      for (int rep = 0; rep < 4; ++rep) {  // rep 0 warms up
+        MVD_CHECK(cudaEventRecord(e0, h->stream));
+        launch_fwd_mirror(h->pt, *p, h->psi.as<float>(), spec.as<float2>(), h->stream);
+        launch_z(h->pt, *p, spec.as<float2>(), otf.as<float2>(), h->stream);
+        launch_inv_quotient(h->pt, *p, spec.as<float2>(), h->img[v].as<float>(), h->q.as<float>(), h->stream);
+        launch_fwd_value(h->pt, *p, h->q.as<float>(), 1.f, spec.as<float2>(), h->stream);
+        launch_z(h->pt, *p, spec.as<float2>(), otf.as<float2>(), h->stream);
+        launch_inv_quotient(h->pt, *p, spec.as<float2>(), h->img[v].as<float>(), h->q.as<float>(), h->stream);
+        MVD_CHECK(cudaEventRecord(e1, h->stream));
+        MVD_CHECK(cudaEventSynchronize(e1));
+        float t = 0.f;
+        MVD_CHECK(cudaEventElapsedTime(&t, e0, e1));
+        if (rep > 0) ms_t = std::min(ms_t, t);
+      }
+      if (ms_t < ms) {
+        ms = ms_t;
+        best_threads = threads;
+      }
     }
+    p->threads_plane = best_threads;
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     if (ms < best_ms) {

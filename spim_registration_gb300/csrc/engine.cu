@@ -217,6 +217,15 @@ int plane_cap() {
   return cap;
 }
 
+int plane_threads() {
+  static int t = [] {
+    const char* e = std::getenv("MVD_PLANE_THREADS");
+    int v = e ? std::atoi(e) : 0;
+    return (v >= 64 && v <= kThreads && v % 32 == 0) ? v : kThreads;
+  }();
+  return t;
+}
+
 std::unique_ptr<ConvPlan> make_conv_plan(PlanTable& pt, int nx, int ny, int nz, int kx, int ky,
                                          int kz, const PlanOptions& opt) {
   if (nx < 1 || ny < 1 || nz < 1) throw std::invalid_argument("empty volume");
@@ -290,6 +299,7 @@ std::unique_ptr<ConvPlan> make_conv_plan(PlanTable& pt, int nx, int ny, int nz, 
   p.spec_elems = off;
   p.otf_elems = tile_spec;
   p.smem_plane = 2 * (size_t)by.T * pitch * sizeof(float2);
+  p.threads_plane = opt.threads > 0 ? opt.threads : plane_threads();
   p.smem_z = 2 * (size_t)bz.T * kZPitch * sizeof(float2);
   fill_items(p);
   p.upload();

@@ -78,6 +78,7 @@ struct ConvPlan {
   long long spec_elems = 0;            // complex elements of all tile spectra
   long long otf_elems = 0;             // complex elements of one OTF (all tiles share the shape)
   size_t smem_plane = 0, smem_z = 0;
+  int threads_plane = 0;               // CTA size of the plane kernels (a multiple of 32, <= kThreads)
   DevBuf d_tiles, d_items_fwd, d_items_inv, d_items_z;
   // one tile of this shape at the origin and its work items: the OTF build's tables
   DevBuf d_otf_tile, d_otf_fwd, d_otf_z;
@@ -89,6 +90,7 @@ struct ConvPlan {
 struct PlanOptions {
   int force_tx = 0, force_ty = 0, force_tz = 0;  // 0 = planner's choice
   int cap = 0;                                   // plane-buffer budget; 0 = plane_cap()
+  int threads = 0;                               // plane CTA size; 0 = plane_threads()
 };
 
 // Move a plan's tiles by (dx, dy, dz) into the frame of a larger volume `vol` whose data box
@@ -101,6 +103,8 @@ std::unique_ptr<ConvPlan> make_conv_plan(PlanTable& pt, int nx, int ny, int nz, 
 
 // Planner's budget for one plane buffer (complex values).
 int plane_cap();
+// Default CTA size of the plane kernels (MVD_PLANE_THREADS overrides it).
+int plane_threads();
 
 // Describe the plan for logs.
 std::string describe(const ConvPlan& p);

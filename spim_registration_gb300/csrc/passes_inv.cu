@@ -8,8 +8,9 @@ static void launch_inv_impl(PlanTable& pt, const ConvPlan& p, const float2* spec
   if (p.items_inv.empty()) return;
   auto k = plane_inv_kernel<Epi>;
   set_smem(k, p.smem_plane);
-  k<<<(int)p.items_inv.size(), kThreads, p.smem_plane, s>>>(p.d_tiles.as<TileDesc>(), p.d_items_inv.as<int2>(),
-                                                             pt.device(), spec, e);
+  const int threads = p.threads_plane > 0 ? p.threads_plane : kThreads;
+  k<<<(int)p.items_inv.size(), threads, p.smem_plane, s>>>(p.d_tiles.as<TileDesc>(), p.d_items_inv.as<int2>(),
+                                                            pt.device(), spec, e);
   MVD_CHECK(cudaGetLastError());
   count_launch();
 }
@@ -42,7 +43,8 @@ void launch_inv_store_items(PlanTable& pt, const ConvPlan& p, const TileDesc* ti
   if (nitems == 0) return;
   auto k = plane_inv_kernel<EpiStore>;
   set_smem(k, p.smem_plane);
-  k<<<nitems, kThreads, p.smem_plane, s>>>(tiles, items, pt.device(), spec, EpiStore{out, nx, ny});
+  k<<<nitems, p.threads_plane > 0 ? p.threads_plane : kThreads, p.smem_plane, s>>>(tiles, items, pt.device(), spec,
+                                                                                   EpiStore{out, nx, ny});
   MVD_CHECK(cudaGetLastError());
   count_launch();
 }
