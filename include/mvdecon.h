@@ -202,6 +202,39 @@ int mvd_normalize_weights(float* const* weights, int num_views, long long n, dou
 int mvd_weight_overlap(const float* const* weights, int num_views, long long n, int num_portions, int* min_views,
                        double* avg_views, int devCUDA, void* stream);
 
+/* ----- separable convolution (the difference-of-Gaussian detector's native library) -----
+ * The JNA interface spim/process/cuda/CUDASeparableConvolution.java:34-46 (loaded from a file
+ * whose name contains "separable": the alias libSeparableConvolutionCUDALib.so of this
+ * library).  convolve_K convolves `image` (imageW x imageH x imageD floats, x fastest) in place
+ * along x, then y, then z, each axis only when its flag is set, with K-tap kernels (the
+ * caller centres shorter kernels in zeros, CUDASeparableConvolutionFunctions.java:253-265):
+ * out[x] = sum_{j=-R..R} in[x + j] k[R - j], R = K / 2, accumulated in float in order of j.
+ * Each pass extends its own input: outofbounds 0 = zero, 1 = outofboundsvalue, 2 = the border
+ * pixel.  Returns nonzero on success (JNA boolean); on failure the image is unchanged and the
+ * reason goes to stderr and mvd_last_error().  devCUDA = -1 (the reference's CPU request)
+ * runs on GPU 0. */
+int convolve_127(float* image, float* kernelX, float* kernelY, float* kernelZ, int imageW, int imageH, int imageD,
+                 int convolveX, int convolveY, int convolveZ, int outofbounds, float outofboundsvalue, int devCUDA);
+int convolve_63(float* image, float* kernelX, float* kernelY, float* kernelZ, int imageW, int imageH, int imageD,
+                int convolveX, int convolveY, int convolveZ, int outofbounds, float outofboundsvalue, int devCUDA);
+int convolve_31(float* image, float* kernelX, float* kernelY, float* kernelZ, int imageW, int imageH, int imageD,
+                int convolveX, int convolveY, int convolveZ, int outofbounds, float outofboundsvalue, int devCUDA);
+int convolve_15(float* image, float* kernelX, float* kernelY, float* kernelZ, int imageW, int imageH, int imageD,
+                int convolveX, int convolveY, int convolveZ, int outofbounds, float outofboundsvalue, int devCUDA);
+int convolve_7(float* image, float* kernelX, float* kernelY, float* kernelZ, int imageW, int imageH, int imageD,
+               int convolveX, int convolveY, int convolveZ, int outofbounds, float outofboundsvalue, int devCUDA);
+/* CUDASeparableConvolution.convolutionCPU (:44): all three axes with kernels of 2 r + 1 taps
+ * (r <= 63).  This library has no CPU code path: it computes on GPU 0. */
+void convolutionCPU(float* image, float* kernelX, float* kernelY, float* kernelZ, int kernelRX, int kernelRY,
+                    int kernelRZ, int imageW, int imageH, int imageD, int outofbounds, float outofboundsvalue);
+/* The same passes on device memory (no counterpart in the reference): `image` and `scratch`
+ * are device buffers of dims_xyz floats; kernels[a] (host, taps[a] odd <= 127 values, NULL =
+ * skip axis a).  *result receives the buffer that holds the output (image or scratch).
+ * Enqueued on `stream`. */
+int mvd_separable_convolve_device(float* image, float* scratch, const float* const* kernels, const int* taps,
+                                  const int* dims_xyz, int outofbounds, float outofboundsvalue, int devCUDA,
+                                  void* stream, float** result);
+
 #ifdef __cplusplus
 }
 #endif

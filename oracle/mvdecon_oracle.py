@@ -560,3 +560,41 @@ def weight_overlap(weights, num_portions):
     for start, loop in divide_into_portions(count.size, num_portions):
         avg += float(count[start:start + loop].sum()) / loop
     return int(count.min()), avg / num_portions
+
+
+# --------------------------------------------------------------------------------------------
+# separable convolution (the difference-of-Gaussian detector's native library)
+# --------------------------------------------------------------------------------------------
+SEP_ZERO, SEP_VALUE, SEP_EXTEND = 0, 1, 2
+
+
+def separable_convolve(image, kernels_xyz, oob, value=0.0):
+    """CUDASeparableConvolution.convolve_K (CUDASeparableConvolution.java:34-46), restated from the
+    behaviour the interface documents (the native SeparableConvolutionCUDALib is an external
+    project, not vendored): in place along x, then y, then z (a None kernel skips its axis);
+    out[x] = sum_{j=-R..R} in[x + j] k[R - j]; each pass extends its own input (0 zero,
+    1 value, 2 border pixel) and is stored as float32.  FP64 accumulation (the checker)."""
+    out = np.asarray(image, dtype=np.float32)
+    for axis_xyz, k in enumerate(kernels_xyz):
+        if k is None:
+            continue
+        ax = out.ndim - 1 - axis_xyz
+        if ax < 0:
+            continue
+        k = np.asarray(k, dtype=np.float64)
+        R = len(k) // 2
+        pad = [(0, 0)] * out.ndim
+        pad[ax] = (R, R)
+        if oob == SEP_EXTEND:
+            p = np.pad(out.astype(np.float64), pad, mode="edge")
+        else:
+            cval = float(np.float32(value)) if oob == SEP_VALUE else 0.0
+            p = np.pad(out.astype(np.float64), pad, mode="constant", constant_values=cval)
+        n = out.shape[ax]
+        acc = np.zeros(out.shape, dtype=np.float64)
+        for m in range(2 * R + 1):
+            sl = [slice(None)] * out.ndim
+            sl[ax] = slice(m, m + n)
+            acc += p[tuple(sl)] * k[2 * R - m]
+        out = acc.astype(np.float32)
+    return out

@@ -16,3 +16,4 @@ from .mvdecon import (  # noqa: F401
     MVDeconvolution,
 )
 from .inputs import WeightNormalizer, WeightType, transform_input  # noqa: F401,E402
+from .separable import CUDASeparableConvolution, CUDASeparableConvolutionFunctions, OutOfBounds  # noqa: F401,E402

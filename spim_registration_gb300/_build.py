@@ -1,8 +1,10 @@
 """Build step of the sm_103a library (nvcc, in-tree, no cmake).
 
 Compiles ``csrc/*.cu`` in parallel for ``sm_103a`` and links ``lib/libFourierConvolutionCUDA.so``
-(CUDA runtime linked statically, so the library needs only the driver), plus the alias
-``libConvolution3D_fftCUDAlib.so`` under which the legacy Fiji plugin loads the same ABI.
+(CUDA runtime linked statically, so the library needs only the driver), plus the aliases
+``libConvolution3D_fftCUDAlib.so`` under which the legacy Fiji plugin loads the same ABI and
+``libSeparableConvolutionCUDALib.so`` (the interest-point detection loads the separable
+convolution from a file whose name contains "separable").
 """
 from __future__ import annotations
 
@@ -16,8 +18,9 @@ PKG = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(PKG, "csrc")
 LIBDIR = os.path.join(PKG, "lib")
 LIBNAME = "libFourierConvolutionCUDA.so"
-ALIAS = "libConvolution3D_fftCUDAlib.so"
-SOURCES = ["engine.cu", "passes_fwd.cu", "passes_inv.cu", "passes_z.cu", "adjoint.cu", "inputs.cu", "capi.cu", "noalloc.cu"]
+ALIASES = ["libConvolution3D_fftCUDAlib.so", "libSeparableConvolutionCUDALib.so"]
+SOURCES = ["engine.cu", "passes_fwd.cu", "passes_inv.cu", "passes_z.cu", "adjoint.cu", "inputs.cu", "separable.cu",
+           "capi.cu", "noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2", "-Xptxas", "-O3"]
 
@@ -69,10 +72,11 @@ def build(force: bool = False, verbose: bool = False) -> str:
     lib = library_path()
     if force or jobs or _stale(lib, objs):
         run([nvcc(), *ARCH, "-shared", "-o", lib, *objs])
-    alias = os.path.join(LIBDIR, ALIAS)
-    if os.path.lexists(alias):
-        os.remove(alias)
-    os.symlink(LIBNAME, alias)
+    for name in ALIASES:
+        alias = os.path.join(LIBDIR, name)
+        if os.path.lexists(alias):
+            os.remove(alias)
+        os.symlink(LIBNAME, alias)
     return lib
 
 

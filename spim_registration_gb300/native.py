@@ -79,6 +79,14 @@ SIGNATURES = {
                                              ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_void_p]),
     "mvd_weight_overlap": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int, ctypes.c_longlong, ctypes.c_int,
                                           _I, ctypes.POINTER(ctypes.c_double), ctypes.c_int, ctypes.c_void_p]),
+    **{f"convolve_{k}": (ctypes.c_int, [_F, _F, _F, _F, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                        ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_float, ctypes.c_int])
+       for k in (127, 63, 31, 15, 7)},
+    "convolutionCPU": (None, [_F, _F, _F, _F, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                              ctypes.c_int, ctypes.c_int, ctypes.c_float]),
+    "mvd_separable_convolve_device": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(_F), _I, _I,
+                                                     ctypes.c_int, ctypes.c_float, ctypes.c_int, ctypes.c_void_p,
+                                                     ctypes.POINTER(ctypes.c_void_p)]),
 }
 
 

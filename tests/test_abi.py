@@ -31,9 +31,19 @@ def test_jna_names_of_the_reference_interfaces(lib):
         assert hasattr(lib, n)
 
 
-def test_legacy_alias_points_to_the_library(lib):
-    alias = os.path.join(_build.LIBDIR, _build.ALIAS)
-    assert os.path.realpath(alias) == os.path.realpath(_build.library_path())
+def test_aliases_point_to_the_library(lib):
+    for name in _build.ALIASES:
+        alias = os.path.join(_build.LIBDIR, name)
+        assert os.path.realpath(alias) == os.path.realpath(_build.library_path())
+    # the detection plugin loads the separable library by a name containing "separable"
+    # (DifferenceOfGaussian.java:366-369)
+    assert any("separable" in n.lower() for n in _build.ALIASES)
+
+
+def test_jna_names_of_the_separable_interface(lib):
+    # CUDASeparableConvolution.java:34-46
+    for n in ["convolve_127", "convolve_63", "convolve_31", "convolve_15", "convolve_7", "convolutionCPU"]:
+        assert hasattr(lib, n)
 
 
 def test_device_count_semantics(lib):
