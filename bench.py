@@ -311,6 +311,7 @@ def run_ours(args, rank, world, local):
         out["e2e"] = run_e2e(prob, local, steps=2)
     if rank == 0:
         out["input_preparation"] = run_inputs(prob, local, hbm_peak)
+        out["separable_convolution"] = run_separable(prob, local, hbm_peak)
     if rank == 0 and not args.no_cpu:
         out["cpu_baseline"] = cpu_baseline(prob)
     return out
@@ -400,6 +401,56 @@ def run_inputs(prob, device, hbm_peak, reps=5):
     res["box_xyz"] = [nx, ny, nz]
     res["total_ms"] = round(float(ms.sum()), 4)
     res["note"] = "weight_overlap includes its device-to-host read of the statistics"
+    return res
+
+
+def run_separable(prob, device, hbm_peak, reps=10):
+    """The difference-of-Gaussian detector's separable convolution at the workload's volume
+    size: x, y and z passes with K-tap kernels, device-resident (algorithmic bytes: 8 per voxel
+    and pass), and the JNA call convolve_K on a host array (copies in and out included)."""
+    import torch
+
+    from spim_registration_gb300 import native
+    from spim_registration_gb300.separable import CUDASeparableConvolution
+
+    nz, ny, nx = prob.views[0].shape
+    n = nx * ny * nz
+    lib = native.load()
+    a = torch.from_numpy(np.ascontiguousarray(prob.views[0])).to(f"cuda:{device}")
+    b = torch.empty_like(a)
+    stream = torch.cuda.current_stream(device)
+    res = {"volume_xyz": [nx, ny, nz], "passes": 3}
+    for K in (15, 127):
+        ks = [np.exp(-0.5 * ((np.arange(K) - K // 2) / (K / 6.0)) ** 2).astype(np.float32) for _ in range(3)]
+        kp = (native._F * 3)(*[native.fptr(k) for k in ks])
+        out = native.ctypes.c_void_p()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+        def run():
+            native.check(lib.mvd_separable_convolve_device(a.data_ptr(), b.data_ptr(), kp, native.iarr([K, K, K]),
+                                                           native.iarr([nx, ny, nz]), 2, 0.0, device,
+                                                           native.ctypes.c_void_p(stream.cuda_stream),
+                                                           native.ctypes.byref(out)))
+        run()
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(reps):
+            run()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / reps
+        gbs = 24.0 * n / (ms / 1e3) / 1e9
+        host = np.ascontiguousarray(prob.views[0]).reshape(-1).copy()
+        cuda = CUDASeparableConvolution()
+        getattr(cuda, f"convolve_{K}")(host, *ks, nx, ny, nz, True, True, True, 2, 0.0, device)
+        t0 = time.perf_counter()
+        for _ in range(3):
+            getattr(cuda, f"convolve_{K}")(host, *ks, nx, ny, nz, True, True, True, 2, 0.0, device)
+        t_host = (time.perf_counter() - t0) / 3
+        res[f"K{K}"] = {"device_ms": round(ms, 4), "gbs": round(gbs, 1), "frac_of_measured_hbm": round(gbs / hbm_peak, 3),
+                        "voxels_per_s": n / (ms / 1e3), "jna_call_ms": round(t_host * 1e3, 3),
+                        "jna_voxels_per_s": n / t_host}
+    res["note"] = "device: 3 passes, 8 B per voxel and pass; jna_call: pageable host array in and out"
     return res
 
 
