@@ -202,6 +202,23 @@ int mvd_normalize_weights(float* const* weights, int num_views, long long n, dou
 int mvd_weight_overlap(const float* const* weights, int num_views, long long n, int num_portions, int* min_views,
                        double* avg_views, int devCUDA, void* stream);
 
+/* ----- PSF pipeline (spim/process/fusion/deconvolution/ExtractPSF.java), on the GPU -----
+ * mvd_extract_psf: ExtractPSF.extractPSFLocal (:374-415): psf[p] = sum over the bead
+ * locations (x, y, z triples, doubles, in the view's pixel frame; host array) of the view
+ * (device, dims_xyz) interpolated trilinearly, extended periodically, at p - psf_dims / 2 +
+ * location; locations are added in the given order.  normalize != 0 then applies
+ * ExtractPSF.normalize (:298-316): (v - min) / (max - min).  psf: device, overwritten. */
+int mvd_extract_psf(const float* img, const int* dims_xyz, const double* locations_xyz, int num_locations,
+                    const int* psf_dims_xyz, float* psf, int normalize, int devCUDA, void* stream);
+/* ExtractPSF.transformPSF (:325-372), host only: the odd size of the transformed PSF (the
+ * bounding box of model applied to [0, dim - 1], (int)extent + 1, made odd) and the offset that
+ * maps the PSF's centre voxel (dim / 2) to the centre of the result. */
+int mvd_transformed_psf_size(const int* psf_dims_xyz, const double* model, int* out_dims_xyz, double* offset_xyz);
+/* ExtractPSF.transform (:417-464): out[p] = psf(model^-1 (p + offset)), trilinear over the PSF
+ * extended with zeros.  `model` is the view's row-packed 3x4 registration; device buffers. */
+int mvd_transform_psf(const float* psf, const int* psf_dims_xyz, const double* model, const int* out_dims_xyz,
+                      const double* offset_xyz, float* out, int devCUDA, void* stream);
+
 /* ----- separable convolution (the difference-of-Gaussian detector's native library) -----
  * The JNA interface spim/process/cuda/CUDASeparableConvolution.java:34-46 (loaded from a file
  * whose name contains "separable": the alias libSeparableConvolutionCUDALib.so of this

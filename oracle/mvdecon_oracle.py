@@ -598,3 +598,71 @@ def separable_convolve(image, kernels_xyz, oob, value=0.0):
             acc += p[tuple(sl)] * k[2 * R - m]
         out = acc.astype(np.float32)
     return out
+
+
+# --------------------------------------------------------------------------------------------
+# PSF pipeline (ExtractPSF)
+# --------------------------------------------------------------------------------------------
+def _trilinear(v, t, periodic):
+    """Trilinear interpolation of v [z, y, x] at positions t (..., 3) = (x, y, z), FP64; the
+    volume is extended periodically or with zeros."""
+    sz, sy, sx = v.shape
+    f = np.floor(t)
+    a = t - f
+    i0 = f.astype(np.int64)
+    out = np.zeros(t.shape[:-1])
+    for c in range(8):
+        b = [(c >> k) & 1 for k in range(3)]
+        idx = [i0[..., k] + b[k] for k in range(3)]
+        w = np.ones(t.shape[:-1])
+        for k in range(3):
+            w = w * (a[..., k] if b[k] else 1 - a[..., k])
+        if periodic:
+            val = v[np.mod(idx[2], sz), np.mod(idx[1], sy), np.mod(idx[0], sx)]
+        else:
+            ok = (idx[0] >= 0) & (idx[1] >= 0) & (idx[2] >= 0) & (idx[0] < sx) & (idx[1] < sy) & (idx[2] < sz)
+            val = np.where(ok, v[np.clip(idx[2], 0, sz - 1), np.clip(idx[1], 0, sy - 1), np.clip(idx[0], 0, sx - 1)], 0)
+        out += w * val
+    return out
+
+
+def extract_psf_local(img, locations_xyz, psf_dims_xyz, normalize=False):
+    """ExtractPSF.extractPSFLocal (ExtractPSF.java:374-415): the sum over the bead locations of the
+    periodically extended image interpolated at p - size / 2 + location; with ``normalize``,
+    ExtractPSF.normalize (:298-316), (v - min) / (max - min)."""
+    v = np.asarray(img, dtype=np.float64)
+    px, py, pz = psf_dims_xyz
+    z, y, x = np.meshgrid(np.arange(pz), np.arange(py), np.arange(px), indexing="ij")
+    base = np.stack([x - px // 2, y - py // 2, z - pz // 2], axis=-1).astype(np.float64)
+    psf = np.zeros((pz, py, px))
+    for loc in locations_xyz:
+        psf += _trilinear(v, base + np.asarray(loc, dtype=np.float64), periodic=True)
+    if normalize:
+        lo, hi = psf.min(), psf.max()
+        psf = (psf - lo) / (hi - lo)
+    return psf
+
+
+def transformed_psf_size(psf_dims_xyz, model_rows):
+    """ExtractPSF.transformPSF (:325-372): odd output size and offset."""
+    a = np.asarray(model_rows, dtype=np.float64).reshape(3, 4)
+    corners = np.array([[(c & 1) * (psf_dims_xyz[0] - 1), ((c >> 1) & 1) * (psf_dims_xyz[1] - 1),
+                         ((c >> 2) & 1) * (psf_dims_xyz[2] - 1)] for c in range(8)], dtype=np.float64)
+    t = corners @ a[:, :3].T + a[:, 3]
+    size = t.max(axis=0) - t.min(axis=0)
+    ns = [int(s) + 1 for s in size]
+    ns = [n + 1 if n % 2 == 0 else n for n in ns]
+    ctr = np.array([d // 2 for d in psf_dims_xyz], dtype=np.float64)
+    tc = a[:, :3] @ ctr + a[:, 3]
+    return ns, [tc[d] - ns[d] // 2 for d in range(3)]
+
+
+def transform_psf(psf, model_rows, out_dims_xyz, offset_xyz):
+    """ExtractPSF.transform (:417-464): out[p] = psf(model^-1 (p + offset)), trilinear, zero outside."""
+    a = np.asarray(model_rows, dtype=np.float64).reshape(3, 4)
+    r_inv = np.linalg.inv(a[:, :3])
+    nx, ny, nz = out_dims_xyz
+    z, y, x = np.meshgrid(np.arange(nz), np.arange(ny), np.arange(nx), indexing="ij")
+    p = np.stack([x + offset_xyz[0], y + offset_xyz[1], z + offset_xyz[2]], axis=-1).astype(np.float64)
+    t = (p - a[:, 3]) @ r_inv.T
+    return _trilinear(np.asarray(psf, dtype=np.float64), t, periodic=False)

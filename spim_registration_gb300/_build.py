@@ -19,7 +19,7 @@ CSRC = os.path.join(PKG, "csrc")
 LIBDIR = os.path.join(PKG, "lib")
 LIBNAME = "libFourierConvolutionCUDA.so"
 ALIASES = ["libConvolution3D_fftCUDAlib.so", "libSeparableConvolutionCUDALib.so"]
-SOURCES = ["engine.cu", "passes_fwd.cu", "passes_inv.cu", "passes_z.cu", "adjoint.cu", "inputs.cu", "separable.cu",
+SOURCES = ["engine.cu", "passes_fwd.cu", "passes_inv.cu", "passes_z.cu", "adjoint.cu", "inputs.cu", "psf.cu", "separable.cu",
            "capi.cu", "noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2", "-Xptxas", "-O3"]

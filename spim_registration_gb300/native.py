@@ -84,6 +84,11 @@ SIGNATURES = {
        for k in (127, 63, 31, 15, 7)},
     "convolutionCPU": (None, [_F, _F, _F, _F, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                               ctypes.c_int, ctypes.c_int, ctypes.c_float]),
+    "mvd_extract_psf": (ctypes.c_int, [ctypes.c_void_p, _I, _D, ctypes.c_int, _I, ctypes.c_void_p, ctypes.c_int,
+                                       ctypes.c_int, ctypes.c_void_p]),
+    "mvd_transformed_psf_size": (ctypes.c_int, [_I, _D, _I, _D]),
+    "mvd_transform_psf": (ctypes.c_int, [ctypes.c_void_p, _I, _D, _I, _D, ctypes.c_void_p, ctypes.c_int,
+                                         ctypes.c_void_p]),
     "mvd_separable_convolve_device": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(_F), _I, _I,
                                                      ctypes.c_int, ctypes.c_float, ctypes.c_int, ctypes.c_void_p,
                                                      ctypes.POINTER(ctypes.c_void_p)]),
