@@ -226,6 +226,14 @@ int plane_threads() {
   return t;
 }
 
+bool use_fixed_planes() {
+  static bool on = [] {
+    const char* e = std::getenv("MVD_FIXED_PLANES");
+    return !(e && e[0] == '0');
+  }();
+  return on;
+}
+
 std::unique_ptr<ConvPlan> make_conv_plan(PlanTable& pt, int nx, int ny, int nz, int kx, int ky,
                                          int kz, const PlanOptions& opt) {
   if (nx < 1 || ny < 1 || nz < 1) throw std::invalid_argument("empty volume");

@@ -105,6 +105,9 @@ std::unique_ptr<ConvPlan> make_conv_plan(PlanTable& pt, int nx, int ny, int nz, 
 int plane_cap();
 // Default CTA size of the plane kernels (MVD_PLANE_THREADS overrides it).
 int plane_threads();
+// Whether compiled tile shapes use their compile-time-shaped plane kernels (MVD_FIXED_PLANES=0
+// selects the generic kernels everywhere).
+bool use_fixed_planes();
 
 // Describe the plan for logs.
 std::string describe(const ConvPlan& p);

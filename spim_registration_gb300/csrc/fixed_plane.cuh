@@ -1,0 +1,225 @@
+// Plane kernels with the tile shape fixed at compile time.
+//
+// The generic plane kernels (kernels.cuh) read the tile lengths, radices and strides from
+// their plan at run time, so every stage carries index arithmetic on runtime values and the
+// kernel carries every radix (a large body that misses the instruction cache).  For the tile
+// shapes the planner picks most often, these kernels take (TX, TY, threads) as template
+// parameters: the radix sequence, strides, butterfly counts and the twiddle stride are
+// constants, divisions by them become multiplies, shared-memory offsets become immediates,
+// and only the radices of the shape are compiled in.  The arithmetic (radix order, twiddles,
+// functors, epilogues) is the generic kernels', so results are bit-identical to them.
+#pragma once
+#include "kernels.cuh"
+
+namespace mvd {
+
+// The planner's factorisation (engine.cu factorize): fewest stages, then the largest smallest
+// radix, radices non-increasing, from {16, 15, 12, 10, 8, 6, 5, 4, 3, 2}.
+struct SplitC {
+  int s = 0;
+  int r[kMaxStages] = {0, 0, 0, 0, 0, 0};
+};
+
+constexpr int kRadixList[10] = {16, 15, 12, 10, 8, 6, 5, 4, 3, 2};
+
+__host__ __device__ constexpr int split_min(const SplitC& c) {
+  int m = 1 << 30;
+  for (int i = 0; i < c.s; ++i) m = c.r[i] < m ? c.r[i] : m;
+  return c.s ? m : 0;
+}
+
+__host__ __device__ constexpr void split_search(int n, int depth, int maxdepth, SplitC& cur, SplitC& best, bool& found) {
+  if (n == 1) {
+    if (!found || cur.s < best.s || (cur.s == best.s && split_min(cur) > split_min(best))) {
+      best = cur;
+      found = true;
+    }
+    return;
+  }
+  if (depth == maxdepth) return;
+  for (int i = 0; i < 10; ++i) {
+    const int r = kRadixList[i];
+    if (n % r) continue;
+    if (cur.s && r > cur.r[cur.s - 1]) continue;
+    cur.r[cur.s++] = r;
+    split_search(n / r, depth + 1, maxdepth, cur, best, found);
+    --cur.s;
+  }
+}
+
+__host__ __device__ constexpr SplitC split_of(int n) {
+  SplitC cur{}, best{};
+  bool found = false;
+  if (n == 1) {
+    best.s = 1;
+    best.r[0] = 1;
+    return best;
+  }
+  for (int d = 1; d <= kMaxStages && !found; ++d) split_search(n, 0, d, cur, best, found);
+  return best;
+}
+
+// Shared-memory accessor with compile-time strides: element (batch, i) at
+// p[batch * BS + s(i) * ES], s(i) = i or the skewed i + i/16.
+template <int ES, int BS, bool SKEW>
+struct SmemC {
+  float2* p;
+  __device__ __forceinline__ static int at(int batch, int i) { return batch * BS + (SKEW ? i + (i >> 4) : i) * ES; }
+  template <int R>
+  __device__ __forceinline__ void get(int batch, int j, int NR, float2* v) const {
+    if (SKEW) {
+#pragma unroll
+      for (int r = 0; r < R; ++r) v[r] = p[at(batch, j + r * NR)];
+    } else {
+      const float2* q = p + batch * BS + j * ES;
+#pragma unroll
+      for (int r = 0; r < R; ++r) v[r] = q[r * NR * ES];
+    }
+  }
+  template <int R>
+  __device__ __forceinline__ void put(int batch, int base, int Ns, const float2* v) const {
+    if (SKEW) {
+#pragma unroll
+      for (int r = 0; r < R; ++r) p[at(batch, base + r * Ns)] = v[r];
+    } else {
+      float2* q = p + batch * BS + base * ES;
+#pragma unroll
+      for (int r = 0; r < R; ++r) q[r * Ns * ES] = v[r];
+    }
+  }
+};
+
+// One radix-R Stockham stage over `count` sequences of length N (Ns = product of the earlier
+// radices), T threads; the generic stage_r with N, Ns, R and T constant.
+template <int R, int N, int NS, bool INV, bool JFAST, int T, class LD, class ST>
+__device__ __forceinline__ void stage_c(int count, const float2* __restrict__ tw, const LD& ld, const ST& st) {
+  constexpr int NR = N / R;
+  constexpr int TWS = N / (NS * R);
+  const int nb = count * NR;
+  const int fast = JFAST ? NR : count;
+  for (int b = threadIdx.x; b < nb; b += T) {
+    const int sl = b / fast;
+    const int f = b - sl * fast;
+    const int batch = JFAST ? sl : f;
+    const int j = JFAST ? f : sl;
+    float2 v[R];
+    ld.template get<R>(batch, j, NR, v);
+    const int k = NS > 1 ? j % NS : 0;
+    if (NS > 1 && k != 0) {
+#pragma unroll
+      for (int r = 1; r < R; ++r) {
+        float2 w = __ldg(tw + r * k * TWS);
+        if (INV) w.y = -w.y;
+        v[r] = cmul(v[r], w);
+      }
+    }
+    Dft<R, INV>::run(v);
+    st.template put<R>(batch, (j - k) * R + k, NS, v);
+  }
+}
+
+template <int N>
+__host__ __device__ constexpr int ns_before(int s) {
+  int p = 1;
+  for (int i = 0; i < s; ++i) p *= split_of(N).r[i];
+  return p;
+}
+
+// Stages s .. S-1 of a length-N transform whose result stays in shared memory (the generic
+// run_transform_smem): stage 0 loads with ld0, every stage writes the other buffer.
+template <int N, int s, bool INV, bool ROWS, bool ROW_G0, int ES, int BS, int T, class LD0>
+__device__ __forceinline__ void smem_stages(int count, const float2* __restrict__ tw, const LD0& ld0, float2*& cur,
+                                            float2*& oth) {
+  constexpr SplitC sp = split_of(N);
+  if constexpr (s < sp.s) {
+    constexpr int R = sp.r[s];
+    constexpr int NS = ns_before<N>(s);
+    if constexpr (s == 0) {
+      constexpr bool skew_out = ROWS && ROW_G0 && sp.s > 1;
+      stage_c<R, N, NS, INV, ROWS && ROW_G0, T>(count, tw, ld0, SmemC<ES, BS, skew_out>{oth});
+    } else {
+      constexpr bool skew_in = ROWS && ROW_G0 && s == 1;
+      stage_c<R, N, NS, INV, false, T>(count, tw, SmemC<ES, BS, skew_in>{cur}, SmemC<ES, BS, false>{oth});
+    }
+    __syncthreads();
+    float2* t = cur;
+    cur = oth;
+    oth = t;
+    smem_stages<N, s + 1, INV, ROWS, ROW_G0, ES, BS, T>(count, tw, ld0, cur, oth);
+  }
+}
+
+// All stages with the last storing through stl (the generic run_transform_to).
+template <int N, int s, bool INV, bool ROWS, int ES, int BS, int T, class LD0, class STL>
+__device__ __forceinline__ void to_stages(int count, const float2* __restrict__ tw, const LD0& ld0, const STL& stl,
+                                          float2*& cur, float2*& oth) {
+  constexpr SplitC sp = split_of(N);
+  constexpr int R = sp.r[s];
+  constexpr int NS = ns_before<N>(s);
+  if constexpr (sp.s == 1) {
+    stage_c<R, N, 1, INV, ROWS, T>(count, tw, ld0, stl);
+  } else if constexpr (s == sp.s - 1) {
+    stage_c<R, N, NS, INV, ROWS, T>(count, tw, SmemC<ES, BS, ROWS>{cur}, stl);
+  } else {
+    constexpr bool skew_out = ROWS && s == sp.s - 2;
+    if constexpr (s == 0)
+      stage_c<R, N, NS, INV, false, T>(count, tw, ld0, SmemC<ES, BS, skew_out>{oth});
+    else
+      stage_c<R, N, NS, INV, false, T>(count, tw, SmemC<ES, BS, false>{cur}, SmemC<ES, BS, skew_out>{oth});
+    __syncthreads();
+    float2* t = cur;
+    cur = oth;
+    oth = t;
+    to_stages<N, s + 1, INV, ROWS, ES, BS, T>(count, tw, ld0, stl, cur, oth);
+  }
+}
+
+template <class Gather, int TX, int TY, int T>
+__global__ void __launch_bounds__(T, 2)
+plane_fwd_fixed(const TileDesc* __restrict__ tiles, const int2* __restrict__ items, const FftPlan* __restrict__ plans,
+                float2* __restrict__ spec, Gather gather) {
+  constexpr int M = TX / 2, PX = M + 1, PITCH = row_pitch(M);
+  extern __shared__ float2 sm[];
+  const int2 it = items[blockIdx.x];
+  const TileDesc t = tiles[it.x];
+  const int z = it.y;
+  float2* cur = sm;
+  float2* oth = sm + TY * PITCH;
+  RowGather<Gather, false> ld0{gather, t.ox, t.oy, t.oz + z, 0, 0, 0, 0, true};
+  const FftPlan* pxp = plans + t.plan_x;
+  smem_stages<M, 0, false, true, true, 1, PITCH, T>(TY, pxp->tw, ld0, cur, oth);
+  SpecSliceStore st{spec + t.spec_off + (long long)z * TY * PX, PX};
+  to_stages<TY, 0, false, false, PITCH, 1, T>(PX, plans[t.plan_y].tw, R2CColumnLoad{cur, PITCH, M, pxp->tw_r2c}, st,
+                                             cur, oth);
+}
+
+template <class Epi, int TX, int TY, int T>
+__global__ void __launch_bounds__(T, 2)
+plane_inv_fixed(const TileDesc* __restrict__ tiles, const int2* __restrict__ items, const FftPlan* __restrict__ plans,
+                const float2* __restrict__ spec, Epi epi) {
+  constexpr int M = TX / 2, PX = M + 1, PITCH = row_pitch(M);
+  extern __shared__ float2 sm[];
+  const int2 it = items[blockIdx.x];
+  const TileDesc t = tiles[it.x];
+  const int z = it.y;
+  float2* cur = sm;
+  float2* oth = sm + TY * PITCH;
+  SpecSliceLoad ld{spec + t.spec_off + (long long)z * TY * PX, PX};
+  smem_stages<TY, 0, true, false, false, PITCH, 1, T>(PX, plans[t.plan_y].tw, ld, cur, oth);
+  float2* rows = cur + t.hy * PITCH;
+  float2* rows_oth = oth + t.hy * PITCH;
+  const FftPlan* pxp = plans + t.plan_x;
+  const long long gz = t.oz + z;
+  RowEpilogue<Epi> st{&epi, (gz * epi.ny + (t.oy + t.hy)) * (long long)epi.nx + t.ox + t.hx, (long long)epi.nx,
+                      t.hx, t.ex};
+  epi.acc_init();
+  to_stages<M, 0, true, true, 1, PITCH, T>(t.ey, pxp->tw, C2RRowLoad{rows, PITCH, M, pxp->tw_r2c}, st, rows, rows_oth);
+  epi.finish();
+}
+
+// Tile shapes (x length, y length) with compiled kernels, for 384-thread CTAs.
+#define MVD_FIXED_PLANE_SHAPES(X) \
+  X(100, 100)                     \
+  X(128, 100)
+
+}  // namespace mvd

@@ -33,7 +33,7 @@ constexpr int kZPitch = kZChunk + 1;
 
 // Row pitch (complex values, odd) that holds a half-spectrum row of px = M + 1 values and
 // the skewed layout i + i/16 of a length-M row between the first two row stages.
-__host__ __device__ inline int row_pitch(int M) {
+__host__ __device__ constexpr int row_pitch(int M) {
   int p = M + 1;
   const int skew = M + (M - 1) / 16 + 1;
   if (skew > p) p = skew;

@@ -1,15 +1,36 @@
 // Instantiations and launches of the forward plane pass (split from engine.cu so the library builds in parallel).
 #include "engine.h"
+#include "fixed_plane.cuh"
 
 namespace mvd {
 
+// The compile-time-shaped kernel for (tx, ty) at 384 threads, if one is compiled.
+template <class Gather>
+static bool launch_fwd_fixed(int tx, int ty, int threads, PlanTable& pt, const TileDesc* tiles, const int2* items,
+                             int nitems, size_t smem, float2* spec, Gather g, cudaStream_t s) {
+  if (threads != kThreads || !use_fixed_planes()) return false;
+#define MVD_FWD_CASE(TX, TY)                                                           \
+  if (tx == TX && ty == TY) {                                                          \
+    auto k = plane_fwd_fixed<Gather, TX, TY, kThreads>;                                \
+    set_smem(k, smem);                                                                 \
+    k<<<nitems, kThreads, smem, s>>>(tiles, items, pt.device(), spec, g);              \
+    return true;                                                                       \
+  }
+  MVD_FIXED_PLANE_SHAPES(MVD_FWD_CASE)
+#undef MVD_FWD_CASE
+  return false;
+}
+
 template <class Gather, bool MASK = false>
 static void launch_fwd_impl(PlanTable& pt, const TileDesc* tiles, const int2* items, int nitems, size_t smem,
-                            int threads, float2* spec, Gather g, cudaStream_t s) {
+                            int threads, int tx, int ty, float2* spec, Gather g, cudaStream_t s) {
   if (nitems == 0) return;
-  auto k = plane_fwd_kernel<Gather, MASK>;
-  set_smem(k, smem);
-  k<<<nitems, threads > 0 ? threads : kThreads, smem, s>>>(tiles, items, pt.device(), spec, g);
+  if (MASK || !launch_fwd_fixed(tx, ty, threads > 0 ? threads : kThreads, pt, tiles, items, nitems, smem, spec, g,
+                                s)) {
+    auto k = plane_fwd_kernel<Gather, MASK>;
+    set_smem(k, smem);
+    k<<<nitems, threads > 0 ? threads : kThreads, smem, s>>>(tiles, items, pt.device(), spec, g);
+  }
   MVD_CHECK(cudaGetLastError());
   count_launch();
 }
@@ -17,7 +38,7 @@ static void launch_fwd_impl(PlanTable& pt, const TileDesc* tiles, const int2* it
 void launch_fwd_mirror(PlanTable& pt, const ConvPlan& p, const float* vol, float2* spec, cudaStream_t s) {
   GatherMirror g{{vol, p.vol[0], p.vol[1], p.vol[2]}};
   launch_fwd_impl(pt, p.d_tiles.as<TileDesc>(), p.d_items_fwd.as<int2>(), (int)p.items_fwd.size(), p.smem_plane,
-                  p.threads_plane, spec, g, s);
+                  p.threads_plane, p.ax.T, p.ay.T, spec, g, s);
 }
 
 void launch_fwd_value(PlanTable& pt, const ConvPlan& p, const float* vol, float value, float2* spec,
@@ -25,19 +46,19 @@ void launch_fwd_value(PlanTable& pt, const ConvPlan& p, const float* vol, float 
   GatherValue g = GatherValue::box(vol, p.vol[0], p.vol[1], p.vol[2], value, p.box_lo[0], p.box_lo[1], p.box_lo[2],
                                    p.box_hi[0], p.box_hi[1], p.box_hi[2]);
   launch_fwd_impl(pt, p.d_tiles.as<TileDesc>(), p.d_items_fwd.as<int2>(), (int)p.items_fwd.size(), p.smem_plane,
-                  p.threads_plane, spec, g, s);
+                  p.threads_plane, p.ax.T, p.ay.T, spec, g, s);
 }
 
 void launch_fwd_value_items(PlanTable& pt, const ConvPlan& p, const TileDesc* tiles, const int2* items, int nitems,
                             const float* vol, int vx, int vy, int vz, float value, float2* spec, cudaStream_t s) {
   GatherValue g = GatherValue::full(vol, vx, vy, vz, value);
-  launch_fwd_impl(pt, tiles, items, nitems, p.smem_plane, p.threads_plane, spec, g, s);
+  launch_fwd_impl(pt, tiles, items, nitems, p.smem_plane, p.threads_plane, p.ax.T, p.ay.T, spec, g, s);
 }
 
 void launch_fwd_masked(PlanTable& pt, const ConvPlan& p, const float* vol, float2* spec, cudaStream_t s) {
   GatherValue g = GatherValue::full(vol, p.vol[0], p.vol[1], p.vol[2], 0.f);
   launch_fwd_impl<GatherValue, true>(pt, p.d_tiles.as<TileDesc>(), p.d_items_fwd.as<int2>(), (int)p.items_fwd.size(),
-                                     p.smem_plane, p.threads_plane, spec, g, s);
+                                     p.smem_plane, p.threads_plane, p.ax.T, p.ay.T, spec, g, s);
 }
 
 }  // namespace mvd

@@ -1,16 +1,39 @@
 // Instantiations and launches of the inverse plane pass (split from engine.cu so the library builds in parallel).
 #include "engine.h"
+#include "fixed_plane.cuh"
 
 namespace mvd {
+
+// The compile-time-shaped kernel for the plan's tile shape at 384 threads, if one is compiled.
+template <class Epi>
+static bool launch_inv_fixed(PlanTable& pt, const ConvPlan& p, const TileDesc* tiles, const int2* items, int nitems,
+                             const float2* spec, Epi e, cudaStream_t s) {
+  const int threads = p.threads_plane > 0 ? p.threads_plane : kThreads;
+  if (threads != kThreads || !use_fixed_planes()) return false;
+  const int tx = p.ax.T, ty = p.ay.T;
+#define MVD_INV_CASE(TX, TY)                                                           \
+  if (tx == TX && ty == TY) {                                                          \
+    auto k = plane_inv_fixed<Epi, TX, TY, kThreads>;                                   \
+    set_smem(k, p.smem_plane);                                                         \
+    k<<<nitems, kThreads, p.smem_plane, s>>>(tiles, items, pt.device(), spec, e);      \
+    return true;                                                                       \
+  }
+  MVD_FIXED_PLANE_SHAPES(MVD_INV_CASE)
+#undef MVD_INV_CASE
+  return false;
+}
 
 template <class Epi>
 static void launch_inv_impl(PlanTable& pt, const ConvPlan& p, const float2* spec, Epi e, cudaStream_t s) {
   if (p.items_inv.empty()) return;
-  auto k = plane_inv_kernel<Epi>;
-  set_smem(k, p.smem_plane);
-  const int threads = p.threads_plane > 0 ? p.threads_plane : kThreads;
-  k<<<(int)p.items_inv.size(), threads, p.smem_plane, s>>>(p.d_tiles.as<TileDesc>(), p.d_items_inv.as<int2>(),
-                                                            pt.device(), spec, e);
+  const int nitems = (int)p.items_inv.size();
+  if (!launch_inv_fixed(pt, p, p.d_tiles.as<TileDesc>(), p.d_items_inv.as<int2>(), nitems, spec, e, s)) {
+    auto k = plane_inv_kernel<Epi>;
+    set_smem(k, p.smem_plane);
+    const int threads = p.threads_plane > 0 ? p.threads_plane : kThreads;
+    k<<<nitems, threads, p.smem_plane, s>>>(p.d_tiles.as<TileDesc>(), p.d_items_inv.as<int2>(), pt.device(), spec,
+                                            e);
+  }
   MVD_CHECK(cudaGetLastError());
   count_launch();
 }
@@ -41,10 +64,12 @@ void launch_inv_nll(PlanTable& pt, const ConvPlan& p, const float2* spec, const 
 void launch_inv_store_items(PlanTable& pt, const ConvPlan& p, const TileDesc* tiles, const int2* items, int nitems,
                             const float2* spec, float* out, int nx, int ny, cudaStream_t s) {
   if (nitems == 0) return;
-  auto k = plane_inv_kernel<EpiStore>;
-  set_smem(k, p.smem_plane);
-  k<<<nitems, p.threads_plane > 0 ? p.threads_plane : kThreads, p.smem_plane, s>>>(tiles, items, pt.device(), spec,
-                                                                                   EpiStore{out, nx, ny});
+  if (!launch_inv_fixed(pt, p, tiles, items, nitems, spec, EpiStore{out, nx, ny}, s)) {
+    auto k = plane_inv_kernel<EpiStore>;
+    set_smem(k, p.smem_plane);
+    k<<<nitems, p.threads_plane > 0 ? p.threads_plane : kThreads, p.smem_plane, s>>>(tiles, items, pt.device(), spec,
+                                                                                     EpiStore{out, nx, ny});
+  }
   MVD_CHECK(cudaGetLastError());
   count_launch();
 }
