@@ -217,6 +217,105 @@ plane_inv_fixed(const TileDesc* __restrict__ tiles, const int2* __restrict__ ite
   epi.finish();
 }
 
+// Forward last stage + product with the OTF + inverse first stage in registers (the generic
+// zmid_r) for a length-N pencil with radix R = the last forward radix.
+template <int R, int N, int T, class LD, class MUL, class ST>
+__device__ __forceinline__ void zmid_c(int count, const float2* __restrict__ tw, const LD& ld, const MUL& mul,
+                                       const ST& st) {
+  constexpr int NR = N / R;
+  const int nb = count * NR;
+  for (int b = threadIdx.x; b < nb; b += T) {
+    const int j = b / count;
+    const int batch = b - j * count;
+    float2 v[R];
+    ld.template get<R>(batch, j, NR, v);
+    if (j != 0) {
+#pragma unroll
+      for (int r = 1; r < R; ++r) v[r] = cmul(v[r], __ldg(tw + r * j));
+    }
+    Dft<R, false>::run(v);
+    mul.template apply<R>(batch, j, NR, v);
+    Dft<R, true>::run(v);
+    st.template put<R>(batch, j * R, 1, v);
+  }
+}
+
+// Forward stages 1 .. S-2 of the z pencils (stage 0 is done by the caller), shared to shared.
+template <int N, int s, int T>
+__device__ __forceinline__ void z_fwd_stages(int count, const float2* __restrict__ tw, float2*& cur, float2*& oth) {
+  constexpr SplitC sp = split_of(N);
+  if constexpr (s < sp.s - 1) {
+    stage_c<sp.r[s], N, ns_before<N>(s), false, false, T>(count, tw, SmemC<kZPitch, 1, false>{cur},
+                                                          SmemC<kZPitch, 1, false>{oth});
+    float2* t = cur;
+    cur = oth;
+    oth = t;
+    __syncthreads();
+    z_fwd_stages<N, s + 1, T>(count, tw, cur, oth);
+  }
+}
+
+// Inverse stages i = 1 .. S-1 (radices in reverse order); the last stores through g.
+template <int N, int i, int T, class G>
+__device__ __forceinline__ void z_inv_stages(int count, const float2* __restrict__ tw, const G& g, float2*& cur,
+                                             float2*& oth) {
+  constexpr SplitC sp = split_of(N);
+  if constexpr (i < sp.s) {
+    constexpr int R = sp.r[sp.s - 1 - i];
+    // Ns = the product of the radices already inverted: r[S-1] ... r[S-i]
+    constexpr int NS = N / ns_before<N>(sp.s - i);
+    if constexpr (i == sp.s - 1) {
+      stage_c<R, N, NS, true, false, T>(count, tw, SmemC<kZPitch, 1, false>{cur}, g);
+    } else {
+      stage_c<R, N, NS, true, false, T>(count, tw, SmemC<kZPitch, 1, false>{cur}, SmemC<kZPitch, 1, false>{oth});
+      __syncthreads();
+      float2* t = cur;
+      cur = oth;
+      oth = t;
+      z_inv_stages<N, i + 1, T>(count, tw, g, cur, oth);
+    }
+  }
+}
+
+// The z pass of a convolution (forward z, times the OTF, inverse z: the generic zpass_kernel
+// in MODE 0) with the pencil length TZ fixed at compile time.
+template <int TZ, int OCC>
+__global__ void __launch_bounds__(kZThreads, OCC)
+zpass_fixed(const TileDesc* __restrict__ tiles, const int2* __restrict__ items, const FftPlan* __restrict__ plans,
+            float2* __restrict__ spec, const float2* __restrict__ otf) {
+  constexpr SplitC sp = split_of(TZ);
+  extern __shared__ float2 sm[];
+  const int2 it = items[blockIdx.x];
+  const TileDesc t = tiles[it.x];
+  const int p0 = it.y;
+  const long long plane = (long long)t.ty * t.px;
+  const int count = min(kZChunk, (int)(plane - p0));
+  const float2* tw = plans[t.plan_z].tw;
+  float2* cur = sm;
+  float2* oth = sm + TZ * kZPitch;
+  PencilRef g{spec + t.spec_off + p0, plane};
+  OtfMul mul{otf + t.otf_off + p0, plane};
+  if constexpr (sp.s == 1) {
+    zmid_c<sp.r[0], TZ, kZThreads>(count, tw, g, mul, g);
+  } else {
+    // forward stage 0 straight from the pencils into `cur`, then the shared stages
+    stage_c<sp.r[0], TZ, 1, false, false, kZThreads>(count, tw, g, SmemC<kZPitch, 1, false>{cur});
+    __syncthreads();
+    z_fwd_stages<TZ, 1, kZThreads>(count, tw, cur, oth);
+    zmid_c<sp.r[sp.s - 1], TZ, kZThreads>(count, tw, SmemC<kZPitch, 1, false>{cur}, mul, SmemC<kZPitch, 1, false>{oth});
+    __syncthreads();
+    float2* tmp = cur;
+    cur = oth;
+    oth = tmp;
+    z_inv_stages<TZ, 1, kZThreads>(count, tw, g, cur, oth);
+  }
+}
+
+// Pencil lengths with compiled z-pass kernels.
+#define MVD_FIXED_Z_LENGTHS(X) \
+  X(240)                       \
+  X(216)
+
 // Tile shapes (x length, y length) with compiled kernels, for 384-thread CTAs.
 #define MVD_FIXED_PLANE_SHAPES(X) \
   X(100, 100)                     \

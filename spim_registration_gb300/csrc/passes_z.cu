@@ -2,6 +2,7 @@
 #include <cstdlib>
 
 #include "engine.h"
+#include "fixed_plane.cuh"
 
 namespace mvd {
 
@@ -15,8 +16,30 @@ static int z_occupancy() {
   return occ;
 }
 
+// The compile-time-length z pass for the plan's pencil length, if one is compiled.
+static bool launch_z_fixed(PlanTable& pt, const ConvPlan& p, float2* spec, const float2* otf, cudaStream_t s) {
+  if (!use_fixed_planes() || z_occupancy() != 3) return false;
+  const int tz = p.az.T;
+#define MVD_Z_CASE(TZ)                                                                                       \
+  if (tz == TZ) {                                                                                            \
+    auto k = zpass_fixed<TZ, 3>;                                                                             \
+    set_smem(k, p.smem_z);                                                                                   \
+    k<<<(int)p.items_z.size(), kZThreads, p.smem_z, s>>>(p.d_tiles.as<TileDesc>(), p.d_items_z.as<int2>(), \
+                                                          pt.device(), spec, otf);                          \
+    return true;                                                                                             \
+  }
+  MVD_FIXED_Z_LENGTHS(MVD_Z_CASE)
+#undef MVD_Z_CASE
+  return false;
+}
+
 void launch_z(PlanTable& pt, const ConvPlan& p, float2* spec, const float2* otf, cudaStream_t s) {
   if (p.items_z.empty()) return;
+  if (launch_z_fixed(pt, p, spec, otf, s)) {
+    MVD_CHECK(cudaGetLastError());
+    count_launch();
+    return;
+  }
   auto k = z_occupancy() == 3 ? zpass_kernel<0, 3> : zpass_kernel<0, 2>;
   set_smem(k, p.smem_z);
   k<<<(int)p.items_z.size(), kZThreads, p.smem_z, s>>>(p.d_tiles.as<TileDesc>(), p.d_items_z.as<int2>(), pt.device(),
