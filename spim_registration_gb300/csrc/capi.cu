@@ -339,7 +339,17 @@ std::vector<Block> divide_into_blocks(const int img[3], const int k[3], const in
 
 }  // namespace
 
+// Owns the handle's stream.  Declared first in mvd_decon, so it is destroyed last: every
+// buffer of the handle is freed in this stream's order before the stream goes away.
+struct StreamHolder {
+  cudaStream_t s = nullptr;
+  ~StreamHolder() {
+    if (s) cudaStreamDestroy(s);
+  }
+};
+
 struct mvd_decon {
+  StreamHolder stream_holder;
   int dev = 0;
   cudaStream_t stream = nullptr;
   PlanTable pt;
@@ -368,7 +378,6 @@ struct mvd_decon {
 
   ~mvd_decon() {
     if (graph) cudaGraphExecDestroy(graph);
-    if (stream) cudaStreamDestroy(stream);
   }
 
   // forward/backward of the image-formation model (allocated on first use)
@@ -546,7 +555,7 @@ void prepare_kernels(mvd_decon* h) {
       mirror(A.as<float>(), dv, k2);
     }
   }
-  MVD_CHECK(cudaStreamSynchronize(s));  // the scratch buffers and plans go out of scope
+  // the scratch buffers and plans go out of scope: freed in the stream's order
 }
 
 // A view's convolutions only need to cover the bounding box of its data or weight (img > 0
@@ -650,6 +659,10 @@ extern "C" int mvd_create(mvd_decon** out, int devCUDA, const int* dims, int num
   auto h = std::make_unique<mvd_decon>();
   h->dev = devCUDA;
   MVD_CHECK(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+  h->stream_holder.s = h->stream;
+  // the handle's buffers, plans and temporaries come from the device pool in stream order
+  keep_pool_memory(devCUDA);
+  AllocScope scope(h->stream);
   for (int d = 0; d < 3; ++d) h->dims[d] = dims[d];
   h->N = (long long)dims[0] * dims[1] * dims[2];
   h->V = num_views;
@@ -819,12 +832,13 @@ extern "C" int mvd_get_psi(mvd_decon* h, float* psi, int masked) {
   MVD_CHECK(cudaSetDevice(h->dev));
   const size_t nb = h->N * sizeof(float);
   if (masked) {
-    DevBuf m(nb);
-    MVD_CHECK(cudaMemcpyAsync(m.p, h->psi.p, nb, cudaMemcpyDeviceToDevice, h->stream));
+    // the quotient buffer is idle between view stages (every stage rewrites it before use):
+    // the masked copy is staged there instead of in a fresh allocation
+    MVD_CHECK(cudaMemcpyAsync(h->q.p, h->psi.p, nb, cudaMemcpyDeviceToDevice, h->stream));
     std::vector<const float*> vp;
     for (int v = 0; v < h->V; ++v) vp.push_back(h->img[v].as<float>());
-    dev_mask(m.as<float>(), vp.data(), h->V, h->N, h->stream);
-    MVD_CHECK(cudaMemcpyAsync(psi, m.p, nb, cudaMemcpyDeviceToHost, h->stream));
+    dev_mask(h->q.as<float>(), vp.data(), h->V, h->N, h->stream);
+    MVD_CHECK(cudaMemcpyAsync(psi, h->q.p, nb, cudaMemcpyDeviceToHost, h->stream));
     MVD_CHECK(cudaStreamSynchronize(h->stream));
   } else {
     MVD_CHECK(cudaMemcpyAsync(psi, h->psi.p, nb, cudaMemcpyDeviceToHost, h->stream));
@@ -985,6 +999,7 @@ namespace {
 
 void adjoint_setup(mvd_decon* h) {
   if (!h->adj.empty()) return;
+  AllocScope scope(h->stream);
   h->adj.resize(h->V);
   long long ext_max = 0, spec_ext_max = 0, tile_max = 0, otf_max = 0;
   for (int v = 0; v < h->V; ++v) {
@@ -1012,7 +1027,7 @@ void adjoint_setup(mvd_decon* h) {
       tab.insert(tab.end(), ix.begin(), ix.end());
     }
     a.fold_tab.alloc(tab.size() * sizeof(int));
-    MVD_CHECK(cudaMemcpy(a.fold_tab.p, tab.data(), tab.size() * sizeof(int), cudaMemcpyHostToDevice));
+    upload_table(a.fold_tab.p, tab.data(), tab.size() * sizeof(int));
     // one full tile of the view's plan, for the inverse transform of the accumulated spectrum
     const ConvPlan& p = *h->plans[v];
     TileDesc t = p.tiles[0];
@@ -1029,9 +1044,9 @@ void adjoint_setup(mvd_decon* h) {
     a.lag_tile.alloc(sizeof(TileDesc));
     a.lag_items_z.alloc(iz.size() * sizeof(int2));
     a.lag_items_inv.alloc(ii.size() * sizeof(int2));
-    MVD_CHECK(cudaMemcpy(a.lag_tile.p, &t, sizeof(TileDesc), cudaMemcpyHostToDevice));
-    MVD_CHECK(cudaMemcpy(a.lag_items_z.p, iz.data(), iz.size() * sizeof(int2), cudaMemcpyHostToDevice));
-    MVD_CHECK(cudaMemcpy(a.lag_items_inv.p, ii.data(), ii.size() * sizeof(int2), cudaMemcpyHostToDevice));
+    upload_table(a.lag_tile.p, &t, sizeof(TileDesc));
+    upload_table(a.lag_items_z.p, iz.data(), iz.size() * sizeof(int2));
+    upload_table(a.lag_items_inv.p, ii.data(), ii.size() * sizeof(int2));
     a.n_lag_z = (int)iz.size();
     a.n_lag_inv = (int)ii.size();
     tile_max = std::max(tile_max, (long long)p.ax.T * p.ay.T * p.az.T);
@@ -1140,6 +1155,7 @@ extern "C" int mvd_set_kernel(mvd_decon* h, int view, int which, const float* da
   if (!h || !data) return fail(MVD_ERR_ARG, "NULL argument");
   if (view < 0 || view >= h->V || (which != 1 && which != 2)) return fail(MVD_ERR_ARG, "bad view or kernel");
   MVD_CHECK(cudaSetDevice(h->dev));
+  AllocScope scope(h->stream);
   DevBuf& k = which == 1 ? h->k1[view] : h->k2[view];
   MVD_CHECK(cudaMemcpyAsync(k.p, data, vox(h->kd[view]) * sizeof(float), cudaMemcpyHostToDevice, h->stream));
   const ConvPlan& p = *h->plans[view];

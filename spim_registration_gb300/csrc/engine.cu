@@ -6,6 +6,8 @@
 #include <cstdlib>
 #include <cmath>
 #include <cstring>
+#include <cstdint>
+#include <mutex>
 #include <sstream>
 
 #include "engine.h"
@@ -23,25 +25,68 @@ void check_cuda(cudaError_t e, const char* what) {
   }
 }
 
-DevBuf::~DevBuf() {
-  if (p) cudaFree(p);
+namespace {
+thread_local cudaStream_t tls_alloc_stream = nullptr;
 }
+
+AllocScope::AllocScope(cudaStream_t s) : prev_(tls_alloc_stream) { tls_alloc_stream = s; }
+AllocScope::~AllocScope() { tls_alloc_stream = prev_; }
+cudaStream_t alloc_stream() { return tls_alloc_stream; }
+
+void upload_table(void* dst, const void* src, size_t bytes) {
+  if (bytes == 0) return;
+  if (tls_alloc_stream)  // pageable source: staged before the call returns
+    MVD_CHECK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, tls_alloc_stream));
+  else
+    MVD_CHECK(cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice));
+}
+
+void keep_pool_memory(int dev) {
+  static std::mutex mu;
+  static std::vector<bool> done;
+  std::lock_guard<std::mutex> lock(mu);
+  if ((int)done.size() <= dev) done.resize(dev + 1, false);
+  if (done[dev]) return;
+  cudaMemPool_t pool;
+  MVD_CHECK(cudaDeviceGetDefaultMemPool(&pool, dev));
+  uint64_t threshold = UINT64_MAX;
+  MVD_CHECK(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &threshold));
+  done[dev] = true;
+}
+
+void DevBuf::release() {
+  if (p) {
+    if (stream)
+      cudaFreeAsync(p, stream);
+    else
+      cudaFree(p);
+  }
+  p = nullptr;
+  bytes = 0;
+  stream = nullptr;
+}
+DevBuf::~DevBuf() { release(); }
 DevBuf& DevBuf::operator=(DevBuf&& o) noexcept {
   if (this != &o) {
-    if (p) cudaFree(p);
+    release();
     p = o.p;
     bytes = o.bytes;
+    stream = o.stream;
     o.p = nullptr;
     o.bytes = 0;
+    o.stream = nullptr;
   }
   return *this;
 }
 void DevBuf::alloc(size_t b) {
-  if (p) cudaFree(p);
-  p = nullptr;
-  bytes = 0;
+  release();
   if (b == 0) return;
-  MVD_CHECK(cudaMalloc(&p, b));
+  if (tls_alloc_stream) {
+    MVD_CHECK(cudaMallocAsync(&p, b, tls_alloc_stream));
+    stream = tls_alloc_stream;
+  } else {
+    MVD_CHECK(cudaMalloc(&p, b));
+  }
   bytes = b;
 }
 void DevBuf::ensure(size_t b) {
@@ -116,7 +161,7 @@ int PlanTable::index_of(int n) {
     tw[n + k] = make_float2((float)std::cos(a), (float)std::sin(a));
   }
   auto buf = std::make_unique<DevBuf>(tw.size() * sizeof(float2));
-  MVD_CHECK(cudaMemcpy(buf->p, tw.data(), tw.size() * sizeof(float2), cudaMemcpyHostToDevice));
+  upload_table(buf->p, tw.data(), tw.size() * sizeof(float2));
   p.tw = buf->as<float2>();
   p.tw_r2c = buf->as<float2>() + n;
   tw_bufs_.push_back(std::move(buf));
@@ -132,7 +177,7 @@ const FftPlan* PlanTable::device() {
   if (dirty_) {
     // append-only table at a fixed address: entries already in use never change, so kernels
     // (and captured graphs) holding this pointer stay valid while new lengths are added
-    MVD_CHECK(cudaMemcpy(dev_.p, host_.data(), host_.size() * sizeof(FftPlan), cudaMemcpyHostToDevice));
+    upload_table(dev_.p, host_.data(), host_.size() * sizeof(FftPlan));
     dirty_ = false;
   }
   return dev_.as<FftPlan>();
@@ -178,10 +223,10 @@ static void fill_items(ConvPlan& p) {
 
 void ConvPlan::upload() {
   d_tiles.alloc(tiles.size() * sizeof(TileDesc));
-  MVD_CHECK(cudaMemcpy(d_tiles.p, tiles.data(), tiles.size() * sizeof(TileDesc), cudaMemcpyHostToDevice));
+  upload_table(d_tiles.p, tiles.data(), tiles.size() * sizeof(TileDesc));
   auto up = [](DevBuf& b, const std::vector<int2>& v) {
     b.alloc(std::max<size_t>(1, v.size()) * sizeof(int2));
-    if (!v.empty()) MVD_CHECK(cudaMemcpy(b.p, v.data(), v.size() * sizeof(int2), cudaMemcpyHostToDevice));
+    if (!v.empty()) upload_table(b.p, v.data(), v.size() * sizeof(int2));
   };
   up(d_items_fwd, items_fwd);
   up(d_items_inv, items_inv);
@@ -198,7 +243,7 @@ void ConvPlan::upload() {
     for (int z = 0; z < t.tz; ++z) fwd.push_back(make_int2(0, z));
     for (int p0 = 0; p0 < t.ty * t.px; p0 += kZChunk) zz.push_back(make_int2(0, p0));
     d_otf_tile.alloc(sizeof(TileDesc));
-    MVD_CHECK(cudaMemcpy(d_otf_tile.p, &t, sizeof(TileDesc), cudaMemcpyHostToDevice));
+    upload_table(d_otf_tile.p, &t, sizeof(TileDesc));
     up(d_otf_fwd, fwd);
     up(d_otf_z, zz);
     n_otf_fwd = (int)fwd.size();

@@ -27,21 +27,48 @@ bool is_smooth(int n);
 int next_smooth(int n, bool even);
 std::vector<int> factorize(int n);  // radices from {16,15,12,10,8,6,5,4,3,2}, product == n
 
-// Device memory owned by RAII
+// Device memory owned by RAII.  Allocated while an AllocScope is active on this thread, it
+// comes from the device's memory pool in the scope stream's order (cudaMallocAsync) and is
+// freed in that stream's order (cudaFreeAsync): no device-wide synchronisation, and the pool
+// keeps the memory for the next allocation.  Otherwise plain cudaMalloc / cudaFree.
 struct DevBuf {
   void* p = nullptr;
   size_t bytes = 0;
+  cudaStream_t stream = nullptr;  // the allocation's stream (stream-ordered), or none
   DevBuf() = default;
   explicit DevBuf(size_t b) { alloc(b); }
   ~DevBuf();
   DevBuf(const DevBuf&) = delete;
   DevBuf& operator=(const DevBuf&) = delete;
-  DevBuf(DevBuf&& o) noexcept : p(o.p), bytes(o.bytes) { o.p = nullptr; o.bytes = 0; }
+  DevBuf(DevBuf&& o) noexcept : p(o.p), bytes(o.bytes), stream(o.stream) {
+    o.p = nullptr;
+    o.bytes = 0;
+    o.stream = nullptr;
+  }
   DevBuf& operator=(DevBuf&& o) noexcept;
   void alloc(size_t b);
   void ensure(size_t b);  // grow (contents lost) if smaller
+  void release();
   template <class T> T* as() const { return static_cast<T*>(p); }
 };
+
+// Stream-ordered allocation for the DevBufs created on this thread during its lifetime; the
+// stream must outlive them.  Host-to-device uploads of tables go through upload_table(), which is
+// ordered in the same stream (a plain copy could overtake work still using recycled memory).
+class AllocScope {
+ public:
+  explicit AllocScope(cudaStream_t s);
+  ~AllocScope();
+  AllocScope(const AllocScope&) = delete;
+  AllocScope& operator=(const AllocScope&) = delete;
+ private:
+  cudaStream_t prev_;
+};
+cudaStream_t alloc_stream();
+void upload_table(void* dst, const void* src, size_t bytes);
+// Keep freed pool memory cached in this process instead of returning it at every
+// synchronisation (the device's default pool; a process-local attribute).
+void keep_pool_memory(int dev);
 
 // Twiddle tables and FFT plans for every length used on a device.
 class PlanTable {

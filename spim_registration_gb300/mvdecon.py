@@ -203,8 +203,12 @@ class Deconvolution:
     def synchronize(self):
         native.check(self.lib.mvd_synchronize(self.h))
 
-    def get_psi(self, masked: bool = False) -> np.ndarray:
-        out = np.empty(self.shape, dtype=np.float32)
+    def get_psi(self, masked: bool = False, out: np.ndarray | None = None) -> np.ndarray:
+        """psi as float32 [z, y, x]; ``out`` may be a caller-owned (e.g. pinned) array to fill."""
+        if out is None:
+            out = np.empty(self.shape, dtype=np.float32)
+        elif out.shape != tuple(self.shape) or out.dtype != np.float32 or not out.flags.c_contiguous:
+            raise ValueError("out must be a contiguous float32 array of psi's shape")
         native.check(self.lib.mvd_get_psi(self.h, native.fptr(out), 1 if masked else 0))
         return out
 
