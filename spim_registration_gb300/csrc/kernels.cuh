@@ -456,31 +456,6 @@ struct C2RRowLoad {
   }
 };
 
-template <class Epi>
-struct RowEpilogue {  // last inverse x stage: complex n of effective row `batch` = reals 2n, 2n+1
-  Epi* epi;
-  long long row0;     // global index of (tile-local x = hx, effective row 0, slice z)
-  long long ystride;  // global stride of one row
-  int hx, ex;
-  template <int R>
-  __device__ __forceinline__ void put(int batch, int base, int Ns, const float2* v) const {
-    int off[2 * R];
-    float val[2 * R];
-    bool ok[2 * R];
-#pragma unroll
-    for (int r = 0; r < R; ++r) {
-      const int x0 = 2 * (base + r * Ns) - hx;
-      off[2 * r] = x0;
-      off[2 * r + 1] = x0 + 1;
-      val[2 * r] = v[r].x;
-      val[2 * r + 1] = v[r].y;
-      ok[2 * r] = x0 >= 0 && x0 < ex;
-      ok[2 * r + 1] = x0 + 1 >= 0 && x0 + 1 < ex;
-    }
-    epi->template apply<2 * R>(row0 + batch * ystride, off, val, ok);
-  }
-};
-
 // All stages of one transform with the result left in shared memory: on return (after a
 // barrier) `cur` holds it in the plain layout.  Stage 0 loads with ld0 (global memory or
 // `cur`) and every stage writes the other buffer.  ROWS (row transforms, es == 1): stage 0
@@ -592,11 +567,30 @@ plane_inv_kernel(const TileDesc* __restrict__ tiles, const int2* __restrict__ it
   float2* rows_oth = oth + t.hy * t.pitch;
   const FftPlan* pxp = plans + t.plan_x;
   const long long gz = t.oz + z;
-  RowEpilogue<Epi> st{&epi, (gz * epi.ny + (t.oy + t.hy)) * (long long)epi.nx + t.ox + t.hx, (long long)epi.nx,
-                      t.hx, t.ex};
+  // the C2R row transform stays in shared memory (batch-fastest stages), then the epilogue
+  // walks the effective region by whole warps per row, so its global accesses coalesce
+  run_transform_smem<true, true, false>(pxp, t.ey, C2RRowLoad{rows, t.pitch, M, pxp->tw_r2c}, rows, rows_oth, 1,
+                                        t.pitch);
+  const float* f = reinterpret_cast<const float*>(rows) + t.hx;
+  const int lane = threadIdx.x & 31;
   epi.acc_init();
-  run_transform_to<true, true>(pxp, t.ey, C2RRowLoad{rows, t.pitch, M, pxp->tw_r2c}, st, rows, rows_oth, 1,
-                               t.pitch);
+  for (int row = threadIdx.x >> 5; row < t.ey; row += blockDim.x >> 5) {
+    const long long g0 = (gz * epi.ny + (t.oy + t.hy + row)) * (long long)epi.nx + t.ox + t.hx;
+    const float* src = f + row * (2 * t.pitch);
+    for (int x0 = 0; x0 < t.ex; x0 += 128) {
+      int off[4];
+      float val[4];
+      bool ok[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int x = x0 + lane + 32 * u;
+        off[u] = x;
+        ok[u] = x < t.ex;
+        val[u] = ok[u] ? src[x] : 0.f;
+      }
+      epi.template apply<4>(g0, off, val, ok);
+    }
+  }
   epi.finish();
 }
 
