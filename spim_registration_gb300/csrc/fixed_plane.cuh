@@ -342,7 +342,11 @@ zpass_fixed(const TileDesc* __restrict__ tiles, const int2* __restrict__ items, 
   X(240)                       \
   X(216)
 
-// Tile shapes (x length, y length) with compiled kernels, for 384-thread CTAs.
+// CTA size of the compiled-shape plane kernels (they replace the default 384-thread generic
+// kernels: a plan whose CTA size is the default runs them at this size).
+constexpr int kFixedThreads = 512;
+
+// Tile shapes (x length, y length) with compiled kernels.
 #define MVD_FIXED_PLANE_SHAPES(X) \
   X(100, 100)                     \
   X(128, 100)

@@ -11,9 +11,9 @@ static bool launch_fwd_fixed(int tx, int ty, int threads, PlanTable& pt, const T
   if (threads != kThreads || !use_fixed_planes()) return false;
 #define MVD_FWD_CASE(TX, TY)                                                           \
   if (tx == TX && ty == TY) {                                                          \
-    auto k = plane_fwd_fixed<Gather, TX, TY, kThreads>;                                \
+    auto k = plane_fwd_fixed<Gather, TX, TY, kFixedThreads>;                           \
     set_smem(k, smem);                                                                 \
-    k<<<nitems, kThreads, smem, s>>>(tiles, items, pt.device(), spec, g);              \
+    k<<<nitems, kFixedThreads, smem, s>>>(tiles, items, pt.device(), spec, g);         \
     return true;                                                                       \
   }
   MVD_FIXED_PLANE_SHAPES(MVD_FWD_CASE)

@@ -13,9 +13,9 @@ static bool launch_inv_fixed(PlanTable& pt, const ConvPlan& p, const TileDesc* t
   const int tx = p.ax.T, ty = p.ay.T;
 #define MVD_INV_CASE(TX, TY)                                                           \
   if (tx == TX && ty == TY) {                                                          \
-    auto k = plane_inv_fixed<Epi, TX, TY, kThreads>;                                   \
+    auto k = plane_inv_fixed<Epi, TX, TY, kFixedThreads>;                              \
     set_smem(k, p.smem_plane);                                                         \
-    k<<<nitems, kThreads, p.smem_plane, s>>>(tiles, items, pt.device(), spec, e);      \
+    k<<<nitems, kFixedThreads, p.smem_plane, s>>>(tiles, items, pt.device(), spec, e);      \
     return true;                                                                       \
   }
   MVD_FIXED_PLANE_SHAPES(MVD_INV_CASE)
