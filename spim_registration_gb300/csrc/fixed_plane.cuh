@@ -314,8 +314,8 @@ zpass_fixed(const TileDesc* __restrict__ tiles, const int2* __restrict__ items, 
   const int2 it = items[blockIdx.x];
   const TileDesc t = tiles[it.x];
   const int p0 = it.y;
-  const long long plane = (long long)t.ty * t.px;
-  const int count = min(kZChunk, (int)(plane - p0));
+  const int plane = t.ty * t.px;
+  const int count = min(kZChunk, plane - p0);
   const float2* tw = plans[t.plan_z].tw;
   float2* cur = sm;
   float2* oth = sm + TZ * kZPitch;

@@ -361,9 +361,9 @@ struct SpecSliceStore {
   }
 };
 
-struct PencilRef {  // pencil element: batch = pencil in the chunk, i = z
+struct PencilRef {  // pencil element: batch = pencil in the chunk, i = z (32-bit offsets within a tile)
   float2* p;
-  long long plane;
+  int plane;
   template <int R>
   __device__ __forceinline__ void get(int batch, int j, int NR, float2* v) const {
 #pragma unroll
@@ -378,7 +378,7 @@ struct PencilRef {  // pencil element: batch = pencil in the chunk, i = z
 
 struct PencilScaledStore {
   float2* p;
-  long long plane;
+  int plane;
   float scale;
   template <int R>
   __device__ __forceinline__ void put(int batch, int base, int Ns, const float2* v) const {
@@ -389,7 +389,7 @@ struct PencilScaledStore {
 
 struct OtfMul {  // v[r] *= OTF at natural index j + r NR of pencil `batch`
   const float2* p;
-  long long plane;
+  int plane;
   template <int R>
   __device__ __forceinline__ void apply(int batch, int j, int NR, float2* v) const {
     float2 o[R];
@@ -606,8 +606,8 @@ zpass_kernel(const TileDesc* __restrict__ tiles, const int2* __restrict__ items,
   const int2 it = items[blockIdx.x];
   const TileDesc t = tiles[it.x];
   const int p0 = it.y;
-  const long long plane = (long long)t.ty * t.px;
-  const int count = min(kZChunk, (int)(plane - p0));
+  const int plane = t.ty * t.px;
+  const int count = min(kZChunk, plane - p0);
   const FftPlan* pz = plans + t.plan_z;
   float2* cur = sm;
   float2* oth = sm + t.tz * kZPitch;
