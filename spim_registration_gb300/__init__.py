@@ -18,3 +18,4 @@ from .mvdecon import (  # noqa: F401
 from .inputs import WeightNormalizer, WeightType, transform_input  # noqa: F401,E402
 from .separable import CUDASeparableConvolution, CUDASeparableConvolutionFunctions, OutOfBounds  # noqa: F401,E402
 from .psf import ExtractPSF  # noqa: F401,E402
+from .export import Save3dTIFF  # noqa: F401,E402
