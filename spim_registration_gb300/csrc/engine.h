@@ -135,6 +135,8 @@ int plane_threads();
 // Whether compiled tile shapes use their compile-time-shaped plane kernels (MVD_FIXED_PLANES=0
 // selects the generic kernels everywhere).
 bool use_fixed_planes();
+// Slice copies of the forward plane pass whose bounded wait gave up on the current device.
+int tma_timeouts();
 
 // Describe the plan for logs.
 std::string describe(const ConvPlan& p);

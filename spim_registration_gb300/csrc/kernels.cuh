@@ -83,6 +83,14 @@ struct GatherMirror {  // psi extended mirror-single (MVDeconFFTThreads.java:44,
     return Row{v.data + ((long long)mirror_single(gz, v.nz) * v.ny + mirror_single(gy, v.ny)) * v.nx, v.nx};
   }
   __device__ __forceinline__ float operator()(int gx, int gy, int gz) const { return row(gy, gz)(gx); }
+  // for slice copies: the volume slice holding slice gz, and the (x, y) region read as is
+  __device__ __forceinline__ bool slice_source(int gz, int& zsrc) const {
+    zsrc = mirror_single(gz, v.nz);
+    return true;
+  }
+  __device__ __forceinline__ void region(int& x0, int& x1, int& y0, int& y1) const {
+    x0 = 0; x1 = v.nx; y0 = 0; y1 = v.ny;
+  }
 };
 
 struct GatherValue {  // quotient extended with a constant (value 1: MVDeconFFTThreads.java:63,103)
@@ -114,6 +122,14 @@ struct GatherValue {  // quotient extended with a constant (value 1: MVDeconFFTT
     return Row{in ? v.data + ((long long)gz * v.ny + gy) * v.nx : nullptr, lo[0], hi[0], value};
   }
   __device__ __forceinline__ float operator()(int gx, int gy, int gz) const { return row(gy, gz)(gx); }
+  // for slice copies: false when slice gz lies outside the data box (all of it is `value`)
+  __device__ __forceinline__ bool slice_source(int gz, int& zsrc) const {
+    zsrc = gz;
+    return gz >= lo[2] && gz < hi[2];
+  }
+  __device__ __forceinline__ void region(int& x0, int& x1, int& y0, int& y1) const {
+    x0 = lo[0]; x1 = hi[0]; y0 = lo[1]; y1 = hi[1];
+  }
 };
 
 // ------------------------------------------------------------------------------------------

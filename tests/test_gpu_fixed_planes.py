@@ -22,7 +22,13 @@ SCRIPT = textwrap.dedent("""
     sys.path.insert(0, {root!r})
     from spim_registration_gb300 import Deconvolution
     from spim_registration_gb300 import synthetic as S
-    p = S.make_problem(2, shape_xyz=(172, 172, 192), psf_size_xyz=(15, 15, 41), n_blobs=40, iterations=2)
+    if sys.argv[2] == "full":
+        p = S.make_problem(2, shape_xyz=(172, 172, 192), psf_size_xyz=(15, 15, 41), n_blobs=40, iterations=2)
+    else:  # data boxes smaller than the volume in x, y and z, still planned with 100/128-wide tiles
+        p = S.make_problem(2, shape_xyz=(256, 256, 24), psf_size_xyz=(15, 15, 41), n_blobs=40, iterations=2)
+        for img, w in zip(p.views, p.weights):
+            for a in (img, w):
+                a[:, :, :3] = 0; a[:, :, 253:] = 0; a[:, :2, :] = 0; a[:, 254:, :] = 0; a[20:, :, :] = 0
     d = Deconvolution(p.views, p.weights, p.psfs, p.psftype, p.lam)
     d.run(2)
     np.save(sys.argv[1], d.get_psi())
@@ -30,10 +36,10 @@ SCRIPT = textwrap.dedent("""
 """)
 
 
-def _run(out, fixed):
-    env = dict(os.environ, MVD_FIXED_PLANES="1" if fixed else "0")
-    r = subprocess.run([sys.executable, "-c", SCRIPT.format(root=ROOT), out], env=env, capture_output=True, text=True,
-                       timeout=600)
+def _run(out, fixed, case="full", tma=False):
+    env = dict(os.environ, MVD_FIXED_PLANES="1" if fixed else "0", MVD_TMA="1" if tma else "0")
+    r = subprocess.run([sys.executable, "-c", SCRIPT.format(root=ROOT), out, case], env=env, capture_output=True,
+                       text=True, timeout=600)
     assert r.returncode == 0, r.stderr[-2000:]
     return r.stdout.split()
 
@@ -44,4 +50,15 @@ def test_fixed_shape_kernels_equal_the_generic_kernels(tmp_path):
     assert _run(b, False) == shapes
     assert any(t.startswith("100x100x") for t in shapes)  # a compiled plane shape was planned
     assert any(t.endswith("x240") or t.endswith("x216") for t in shapes)  # and a compiled pencil length
+    np.testing.assert_array_equal(np.load(a), np.load(b))
+
+
+@pytest.mark.parametrize("case", ["full", "crop"])
+def test_slice_copy_forward_kernel_equals_the_generic_kernels(tmp_path, case):
+    """The opt-in TMA forward pass (MVD_TMA=1): its fix-up rewrites the mirror-single border and
+    the value outside data boxes smaller than the volume; psi must equal the generic path's."""
+    a, b = str(tmp_path / "tma.npy"), str(tmp_path / "generic.npy")
+    shapes = _run(a, True, case, tma=True)
+    assert _run(b, False, case) == shapes
+    assert any(t.startswith("100x100x") for t in shapes) and any(t.startswith("128x100x") for t in shapes)
     np.testing.assert_array_equal(np.load(a), np.load(b))
