@@ -7,7 +7,9 @@
 #include <cmath>
 #include <cstring>
 #include <cstdint>
+#include <map>
 #include <mutex>
+#include <tuple>
 #include <sstream>
 
 #include "engine.h"
@@ -270,6 +272,58 @@ int plane_threads() {
   }();
   return t;
 }
+
+namespace {
+
+using EncodeTiled = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                 const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                 CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link to the driver library)
+EncodeTiled encode_tiled() {
+  static EncodeTiled fn = [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      return static_cast<EncodeTiled>(nullptr);
+    return reinterpret_cast<EncodeTiled>(p);
+  }();
+  return fn;
+}
+
+}  // namespace
+
+// Tensor map of a float volume [nz][ny][nx] with a (w, h, 1) box; false when the volume does not
+// meet the copy's rules (16-byte aligned base and row stride) or the driver refuses it.
+bool volume_box_map(const float* base, int nx, int ny, int nz, int w, int h, CUtensorMap* out) {
+  static std::mutex mu;
+  static std::map<std::tuple<const float*, int, int, int, int, int>, CUtensorMap> cache;
+  if ((reinterpret_cast<uintptr_t>(base) & 15) || (nx % 4) || w > 256 || h > 256) return false;
+  const auto key = std::make_tuple(base, nx, ny, nz, w, h);
+  std::lock_guard<std::mutex> lock(mu);
+  auto it = cache.find(key);
+  if (it != cache.end()) {
+    *out = it->second;
+    return true;
+  }
+  EncodeTiled enc = encode_tiled();
+  if (!enc) return false;
+  CUtensorMap m;
+  std::memset(&m, 0, sizeof(m));
+  const cuuint64_t dims[3] = {(cuuint64_t)nx, (cuuint64_t)ny, (cuuint64_t)nz};
+  const cuuint64_t strides[2] = {(cuuint64_t)nx * sizeof(float), (cuuint64_t)nx * ny * sizeof(float)};
+  const cuuint32_t box[3] = {(cuuint32_t)w, (cuuint32_t)h, 1};
+  const cuuint32_t estr[3] = {1, 1, 1};
+  if (enc(&m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float*>(base), dims, strides, box, estr,
+          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+    return false;
+  cache[key] = m;
+  *out = m;
+  return true;
+}
+
 
 bool use_fixed_planes() {
   static bool on = [] {

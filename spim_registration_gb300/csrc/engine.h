@@ -1,5 +1,6 @@
 // Host side of the tiled FFT convolution engine (internal C++ API; the C ABI is in capi.cu).
 #pragma once
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -137,6 +138,9 @@ int plane_threads();
 bool use_fixed_planes();
 // Slice copies of the forward plane pass whose bounded wait gave up on the current device.
 int tma_timeouts();
+// Tensor map of a float volume [nz][ny][nx] with a (w, h, 1) box (cached); false when the volume
+// does not meet the tensor copy's rules (16-byte aligned base and row stride, box <= 256).
+bool volume_box_map(const float* base, int nx, int ny, int nz, int w, int h, CUtensorMap* out);
 
 // Describe the plan for logs.
 std::string describe(const ConvPlan& p);

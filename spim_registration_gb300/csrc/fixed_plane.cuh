@@ -9,9 +9,26 @@
 // and only the radices of the shape are compiled in.  The arithmetic (radix order, twiddles,
 // functors, epilogues) is the generic kernels', so results are bit-identical to them.
 #pragma once
+#include <cuda.h>  // CUtensorMap
+
 #include "kernels.cuh"
 
 namespace mvd {
+
+// Tensor maps of the volumes an epilogue reads, with a box of one effective slice of a tile
+// (x start rounded down to 16 bytes): the inverse pass prefetches them into L2 at its start,
+// so the epilogue's loads, issued after the inverse FFT stages, find them there.
+struct EpiBoxes {
+  CUtensorMap map[2];
+  int count;
+};
+
+__device__ __forceinline__ void prefetch_box_l2(const CUtensorMap* map, int x, int y, int z) {
+  asm volatile("cp.async.bulk.prefetch.tensor.3d.L2.global.tile [%0, {%1, %2, %3}];" ::"l"(
+                   reinterpret_cast<uint64_t>(map)),
+               "r"(x), "r"(y), "r"(z)
+               : "memory");
+}
 
 // The planner's factorisation (engine.cu factorize): fewest stages, then the largest smallest
 // radix, radices non-increasing, from {16, 15, 12, 10, 8, 6, 5, 4, 3, 2}.
@@ -178,15 +195,24 @@ __device__ __forceinline__ void to_stages(int count, const float2* __restrict__ 
 // the volume, j-fastest) with the shape fixed.  Staging the slice in shared memory first, for
 // coalesced warp-per-row loads, measured slower on cfg2 (0.69 vs 0.64 ms per iteration): the
 // j-fastest gather mostly hits L1 and saves a shared-memory pass and a barrier.
+// `src` (count 0 or 1): tensor map of the gathered volume with a (TX rounded to 16 bytes + 4,
+// TY, 1) box; each CTA prefetches into L2 the slice of the CTA `ahead` launches later (one
+// resident wave on), so the next wave's gathers find their rows there.
 template <class Gather, int TX, int TY, int T>
 __global__ void __launch_bounds__(T, 2)
 plane_fwd_fixed(const TileDesc* __restrict__ tiles, const int2* __restrict__ items, const FftPlan* __restrict__ plans,
-                float2* __restrict__ spec, Gather gather) {
+                float2* __restrict__ spec, Gather gather, const __grid_constant__ EpiBoxes src, int ahead) {
   constexpr int M = TX / 2, PX = M + 1, PITCH = row_pitch(M);
   extern __shared__ float2 sm[];
   const int2 it = items[blockIdx.x];
   const TileDesc t = tiles[it.x];
   const int z = it.y;
+  if (threadIdx.x == 0 && src.count && blockIdx.x + ahead < gridDim.x) {
+    const int2 it2 = items[blockIdx.x + ahead];
+    const TileDesc t2 = tiles[it2.x];
+    int zsrc;
+    if (gather.slice_source(t2.oz + it2.y, zsrc)) prefetch_box_l2(&src.map[0], t2.ox & ~3, t2.oy, zsrc);
+  }
   float2* cur = sm;
   float2* oth = sm + TY * PITCH;
   RowGather<Gather, false> ld0{gather, t.ox, t.oy, t.oz + z, 0, 0, 0, 0, true};
@@ -203,12 +229,16 @@ plane_fwd_fixed(const TileDesc* __restrict__ tiles, const int2* __restrict__ ite
 template <class Epi, int TX, int TY, int T>
 __global__ void __launch_bounds__(T, 2)
 plane_inv_fixed(const TileDesc* __restrict__ tiles, const int2* __restrict__ items, const FftPlan* __restrict__ plans,
-                const float2* __restrict__ spec, Epi epi) {
+                const float2* __restrict__ spec, Epi epi, const __grid_constant__ EpiBoxes boxes) {
   constexpr int M = TX / 2, PX = M + 1, PITCH = row_pitch(M);
   extern __shared__ float2 sm[];
   const int2 it = items[blockIdx.x];
   const TileDesc t = tiles[it.x];
   const int z = it.y;
+  // this slice's epilogue inputs (prefetching the next resident wave's as well measured slower:
+  // 27.29 vs 27.57 G voxel-updates/s on cfg2)
+  if (threadIdx.x == 0)
+    for (int i = 0; i < boxes.count; ++i) prefetch_box_l2(&boxes.map[i], (t.ox + t.hx) & ~3, t.oy + t.hy, t.oz + z);
   float2* cur = sm;
   float2* oth = sm + TY * PITCH;
   SpecSliceLoad ld{spec + t.spec_off + (long long)z * TY * PX, PX};

@@ -140,6 +140,7 @@ struct GatherValue {  // quotient extended with a constant (value 1: MVDeconFFTT
 struct EpiStore {
   float* out;
   int nx, ny;
+  int inputs(const float** p) const { return 0; }  // volumes the epilogue reads (for L2 prefetch)
   __device__ __forceinline__ void acc_init() {}
   __device__ __forceinline__ void operator()(long long g, float v) { out[g] = v; }
   template <int K>
@@ -156,6 +157,10 @@ struct EpiQuotient {
   const float* img;
   float* q;
   int nx, ny;
+  int inputs(const float** p) const {
+    p[0] = img;
+    return 1;
+  }
   __device__ __forceinline__ void acc_init() {}
   __device__ __forceinline__ static float quotient(float i, float blurred) {
     return i > 0.f ? __fdiv_rn(i, blurred) : 1.f;
@@ -190,6 +195,11 @@ struct EpiUpdate {
   int nx, ny;
   float acc_sum;
   float acc_max;
+  int inputs(const float** p) const {
+    p[0] = psi;
+    p[1] = weight;
+    return 2;
+  }
   __device__ __forceinline__ void acc_init() {
     acc_sum = 0.f;
     acc_max = 0.f;
@@ -277,6 +287,11 @@ struct EpiNll {
   double* nll;        // += sum over the CTA's voxels
   int nx, ny;
   float acc;
+  int inputs(const float** p) const {
+    p[0] = img;
+    p[1] = weight;
+    return 2;
+  }
   __device__ __forceinline__ void acc_init() { acc = 0.f; }
   __device__ __forceinline__ float term(float f, float im, float w, float& res) {
     if (im > 0.f) {

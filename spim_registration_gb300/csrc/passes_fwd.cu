@@ -16,62 +16,28 @@ namespace mvd {
 
 namespace {
 
-using EncodeTiled = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
-                                 const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
-                                 CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
-
-// cuTensorMapEncodeTiled through the runtime's driver entry point (no link to the driver library)
-EncodeTiled encode_tiled() {
-  static EncodeTiled fn = [] {
-    void* p = nullptr;
-    cudaDriverEntryPointQueryResult q;
-    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
-        q != cudaDriverEntryPointSuccess)
-      return static_cast<EncodeTiled>(nullptr);
-    return reinterpret_cast<EncodeTiled>(p);
+bool use_l2_prefetch() {
+  static bool on = [] {
+    const char* e = std::getenv("MVD_L2_PREFETCH");
+    return !(e && e[0] == '0');
   }();
-  return fn;
+  return on;
 }
 
-// The slice-copy forward kernel is opt-in (MVD_TMA=1): with one slice per CTA the copy's latency
-// stands in front of all of the CTA's work, and on cfg2 it measured slower (0.735 vs 0.62 ms of
-// forward passes per iteration) than the gather that keeps ~20 loads per thread in flight.
+// CTAs of a plane kernel resident at once on the current device (two per SM)
+int resident_ctas() {
+  int dev = 0, sms = 0;
+  MVD_CHECK(cudaGetDevice(&dev));
+  MVD_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  return 2 * sms;
+}
+
 bool use_tma() {
   static bool on = [] {
     const char* e = std::getenv("MVD_TMA");
     return e && e[0] == '1';
   }();
   return on;
-}
-
-// Tensor map of a float volume [nz][ny][nx] with a (w, h, 1) box; false when the volume does not
-// meet the copy's rules (16-byte aligned base and row stride) or the driver refuses it.
-bool volume_box_map(const float* base, int nx, int ny, int nz, int w, int h, CUtensorMap* out) {
-  static std::mutex mu;
-  static std::map<std::tuple<const float*, int, int, int, int, int>, CUtensorMap> cache;
-  if ((reinterpret_cast<uintptr_t>(base) & 15) || (nx % 4) || w > 256 || h > 256) return false;
-  const auto key = std::make_tuple(base, nx, ny, nz, w, h);
-  std::lock_guard<std::mutex> lock(mu);
-  auto it = cache.find(key);
-  if (it != cache.end()) {
-    *out = it->second;
-    return true;
-  }
-  EncodeTiled enc = encode_tiled();
-  if (!enc) return false;
-  CUtensorMap m;
-  std::memset(&m, 0, sizeof(m));
-  const cuuint64_t dims[3] = {(cuuint64_t)nx, (cuuint64_t)ny, (cuuint64_t)nz};
-  const cuuint64_t strides[2] = {(cuuint64_t)nx * sizeof(float), (cuuint64_t)nx * ny * sizeof(float)};
-  const cuuint32_t box[3] = {(cuuint32_t)w, (cuuint32_t)h, 1};
-  const cuuint32_t estr[3] = {1, 1, 1};
-  if (enc(&m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float*>(base), dims, strides, box, estr,
-          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
-          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
-    return false;
-  cache[key] = m;
-  *out = m;
-  return true;
 }
 
 // Per-device count of slice copies whose wait gave up (zero unless a copy never completed).
@@ -111,9 +77,13 @@ static bool launch_fwd_fixed(int tx, int ty, int threads, PlanTable& pt, const T
       set_smem(k, sm);                                                                                    \
       k<<<nitems, kFixedThreads, sm, s>>>(tiles, items, pt.device(), spec, g, map, tma_timeout_counter()); \
     } else {                                                                                              \
+      EpiBoxes src;                                                                                       \
+      std::memset(&src, 0, sizeof(src));                                                                  \
+      src.count = use_l2_prefetch() &&                                                                    \
+                  volume_box_map(g.v.data, g.v.nx, g.v.ny, g.v.nz, tma_box_width(TX), TY, &src.map[0]);   \
       auto k = plane_fwd_fixed<Gather, TX, TY, kFixedThreads>;                                            \
       set_smem(k, smem);                                                                                  \
-      k<<<nitems, kFixedThreads, smem, s>>>(tiles, items, pt.device(), spec, g);                          \
+      k<<<nitems, kFixedThreads, smem, s>>>(tiles, items, pt.device(), spec, g, src, resident_ctas());    \
     }                                                                                                     \
     return true;                                                                                          \
   }

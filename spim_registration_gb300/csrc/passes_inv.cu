@@ -1,8 +1,33 @@
 // Instantiations and launches of the inverse plane pass (split from engine.cu so the library builds in parallel).
+#include <cstdlib>
+#include <cstring>
+
 #include "engine.h"
 #include "fixed_plane.cuh"
 
 namespace mvd {
+
+static bool use_l2_prefetch() {
+  static bool on = [] {
+    const char* e = std::getenv("MVD_L2_PREFETCH");
+    return !(e && e[0] == '0');
+  }();
+  return on;
+}
+
+// Tensor maps for the L2 prefetch of the volumes the epilogue reads (none if any is refused).
+template <class Epi>
+static EpiBoxes epilogue_boxes(const ConvPlan& p, const Epi& e) {
+  EpiBoxes b;
+  std::memset(&b, 0, sizeof(b));
+  const float* in[2] = {nullptr, nullptr};
+  const int n = use_l2_prefetch() ? e.inputs(in) : 0;
+  const int w = (p.ax.E + 3 + 3) / 4 * 4;
+  for (int i = 0; i < n; ++i)
+    if (!volume_box_map(in[i], p.vol[0], p.vol[1], p.vol[2], w, p.ay.E, &b.map[i])) return EpiBoxes{};
+  b.count = n;
+  return b;
+}
 
 // The compile-time-shaped kernel for the plan's tile shape at 384 threads, if one is compiled.
 template <class Epi>
@@ -11,11 +36,12 @@ static bool launch_inv_fixed(PlanTable& pt, const ConvPlan& p, const TileDesc* t
   const int threads = p.threads_plane > 0 ? p.threads_plane : kThreads;
   if (threads != kThreads || !use_fixed_planes()) return false;
   const int tx = p.ax.T, ty = p.ay.T;
+  const EpiBoxes boxes = epilogue_boxes(p, e);
 #define MVD_INV_CASE(TX, TY)                                                           \
   if (tx == TX && ty == TY) {                                                          \
     auto k = plane_inv_fixed<Epi, TX, TY, kFixedThreads>;                              \
     set_smem(k, p.smem_plane);                                                         \
-    k<<<nitems, kFixedThreads, p.smem_plane, s>>>(tiles, items, pt.device(), spec, e);      \
+    k<<<nitems, kFixedThreads, p.smem_plane, s>>>(tiles, items, pt.device(), spec, e, boxes); \
     return true;                                                                       \
   }
   MVD_FIXED_PLANE_SHAPES(MVD_INV_CASE)
