@@ -9,26 +9,9 @@
 // and only the radices of the shape are compiled in.  The arithmetic (radix order, twiddles,
 // functors, epilogues) is the generic kernels', so results are bit-identical to them.
 #pragma once
-#include <cuda.h>  // CUtensorMap
-
 #include "kernels.cuh"
 
 namespace mvd {
-
-// Tensor maps of the volumes an epilogue reads, with a box of one effective slice of a tile
-// (x start rounded down to 16 bytes): the inverse pass prefetches them into L2 at its start,
-// so the epilogue's loads, issued after the inverse FFT stages, find them there.
-struct EpiBoxes {
-  CUtensorMap map[2];
-  int count;
-};
-
-__device__ __forceinline__ void prefetch_box_l2(const CUtensorMap* map, int x, int y, int z) {
-  asm volatile("cp.async.bulk.prefetch.tensor.3d.L2.global.tile [%0, {%1, %2, %3}];" ::"l"(
-                   reinterpret_cast<uint64_t>(map)),
-               "r"(x), "r"(y), "r"(z)
-               : "memory");
-}
 
 // The planner's factorisation (engine.cu factorize): fewest stages, then the largest smallest
 // radix, radices non-increasing, from {16, 15, 12, 10, 8, 6, 5, 4, 3, 2}.

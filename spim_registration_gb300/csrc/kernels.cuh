@@ -20,9 +20,27 @@
 //               rows only (the half-spectrum step folded into the first x stage's loads),
 //               epilogue over the effective (x, y) region (store / quotient / update / NLL).
 #pragma once
+#include <cuda.h>  // CUtensorMap
+
 #include "fft_device.cuh"
 
 namespace mvd {
+
+// Tensor maps of the volumes an epilogue reads, with a box of one effective slice of a tile
+// (x start rounded down to 16 bytes): the inverse pass prefetches them into L2 at its start,
+// so the epilogue's loads, issued after the inverse FFT stages, find them there.
+struct EpiBoxes {
+  CUtensorMap map[2];
+  int count;
+};
+
+__device__ __forceinline__ void prefetch_box_l2(const CUtensorMap* map, int x, int y, int z) {
+  asm volatile("cp.async.bulk.prefetch.tensor.3d.L2.global.tile [%0, {%1, %2, %3}];" ::"l"(
+                   reinterpret_cast<uint64_t>(map)),
+               "r"(x), "r"(y), "r"(z)
+               : "memory");
+}
+
 
 constexpr int kThreads = 384;    // threads per CTA of the plane kernels (two CTAs per SM: 24 warps)
 constexpr int kZThreads = 256;   // threads per CTA of the z-pencil kernel
@@ -555,14 +573,23 @@ __device__ __forceinline__ void run_transform_to(const FftPlan* __restrict__ p, 
 // ------------------------------------------------------------------------------------------
 // MASK: the gathered values are kept only inside the tile's effective region (tiles then
 // partition the volume; used for the PSF gradient's correlation).
+// src (count 0 or 1): tensor map of the gathered volume with a (tx rounded to 16 bytes + 4, ty,
+// 1) box; each CTA prefetches into L2 the slice of the CTA `ahead` launches later.
 template <class Gather, bool MASK = false>
 __global__ void __launch_bounds__(kThreads, 2)
 plane_fwd_kernel(const TileDesc* __restrict__ tiles, const int2* __restrict__ items,
-                 const FftPlan* __restrict__ plans, float2* __restrict__ spec, Gather gather) {
+                 const FftPlan* __restrict__ plans, float2* __restrict__ spec, Gather gather,
+                 const __grid_constant__ EpiBoxes src, int ahead) {
   extern __shared__ float2 sm[];
   const int2 it = items[blockIdx.x];
   const TileDesc t = tiles[it.x];
   const int z = it.y;
+  if (threadIdx.x == 0 && src.count && blockIdx.x + ahead < gridDim.x) {
+    const int2 it2 = items[blockIdx.x + ahead];
+    const TileDesc t2 = tiles[it2.x];
+    int zsrc;
+    if (gather.slice_source(t2.oz + it2.y, zsrc)) prefetch_box_l2(&src.map[0], t2.ox & ~3, t2.oy, zsrc);
+  }
   const int M = t.tx / 2;
   float2* cur = sm;
   float2* oth = sm + t.ty * t.pitch;
@@ -578,14 +605,19 @@ plane_fwd_kernel(const TileDesc* __restrict__ tiles, const int2* __restrict__ it
                                  t.pitch, 1);
 }
 
+// boxes: tensor maps of the volumes the epilogue reads (count 0..2), prefetched into L2 for this
+// slice's effective region at the start
 template <class Epi>
 __global__ void __launch_bounds__(kThreads, 2)
 plane_inv_kernel(const TileDesc* __restrict__ tiles, const int2* __restrict__ items,
-                 const FftPlan* __restrict__ plans, const float2* __restrict__ spec, Epi epi) {
+                 const FftPlan* __restrict__ plans, const float2* __restrict__ spec, Epi epi,
+                 const __grid_constant__ EpiBoxes boxes) {
   extern __shared__ float2 sm[];
   const int2 it = items[blockIdx.x];
   const TileDesc t = tiles[it.x];
   const int z = it.y;  // tile-local slice, inside the effective range
+  if (threadIdx.x == 0)
+    for (int i = 0; i < boxes.count; ++i) prefetch_box_l2(&boxes.map[i], (t.ox + t.hx) & ~3, t.oy + t.hy, t.oz + z);
   const int M = t.tx / 2;
   float2* cur = sm;
   float2* oth = sm + t.ty * t.pitch;

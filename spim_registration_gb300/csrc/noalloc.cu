@@ -267,10 +267,12 @@ extern "C" int mvd_convolve3d_device_noalloc(const float* in, float* out, const 
     place_kernel_noalloc<<<(int)std::min<long long>((kn + 255) / 256, 4096), 256, 0, s>>>(
         kernel, kd[0], kd[1], kd[2], d_place, bx.T, by.T, bz.T);
     MVD_CHECK(cudaGetLastError());
+    EpiBoxes no_boxes;  // no L2 prefetch: no tensor maps are built on this path
+    std::memset(&no_boxes, 0, sizeof(no_boxes));
     smem_attr(plane_fwd_kernel<GatherValue>, smem_plane);
     plane_fwd_kernel<GatherValue><<<(int)otf_fwd.size(), kThreads, smem_plane, s>>>(
         d_tiles, reinterpret_cast<const int2*>(base + o_ofwd), d_plans, d_otf,
-        GatherValue::full(d_place, bx.T, by.T, bz.T, 0.f));
+        GatherValue::full(d_place, bx.T, by.T, bz.T, 0.f), no_boxes, 0);
     MVD_CHECK(cudaGetLastError());
     smem_attr(zpass_kernel<1>, smem_z);
     zpass_kernel<1><<<(int)otf_z.size(), kZThreads, smem_z, s>>>(d_tiles, reinterpret_cast<const int2*>(base + o_oz),
@@ -283,10 +285,10 @@ extern "C" int mvd_convolve3d_device_noalloc(const float* in, float* out, const 
     if (ext_mode == 0) {
       smem_attr(plane_fwd_kernel<GatherMirror>, smem_plane);
       plane_fwd_kernel<GatherMirror><<<(int)fwd.size(), kThreads, smem_plane, s>>>(
-          d_tiles, d_fwd, d_plans, d_spec, GatherMirror{{in, nx, ny, nz}});
+          d_tiles, d_fwd, d_plans, d_spec, GatherMirror{{in, nx, ny, nz}}, no_boxes, 0);
     } else {
       plane_fwd_kernel<GatherValue><<<(int)fwd.size(), kThreads, smem_plane, s>>>(
-          d_tiles, d_fwd, d_plans, d_spec, GatherValue::full(in, nx, ny, nz, ext_value));
+          d_tiles, d_fwd, d_plans, d_spec, GatherValue::full(in, nx, ny, nz, ext_value), no_boxes, 0);
     }
     MVD_CHECK(cudaGetLastError());
     smem_attr(zpass_kernel<0>, smem_z);
@@ -296,7 +298,7 @@ extern "C" int mvd_convolve3d_device_noalloc(const float* in, float* out, const 
     if (!inv.empty()) {
       smem_attr(plane_inv_kernel<EpiStore>, smem_plane);
       plane_inv_kernel<EpiStore><<<(int)inv.size(), kThreads, smem_plane, s>>>(
-          d_tiles, reinterpret_cast<const int2*>(base + o_inv), d_plans, d_spec, EpiStore{out, nx, ny});
+          d_tiles, reinterpret_cast<const int2*>(base + o_inv), d_plans, d_spec, EpiStore{out, nx, ny}, no_boxes);
       MVD_CHECK(cudaGetLastError());
     }
     count_launch(inv.empty() ? 5 : 6);

@@ -98,9 +98,13 @@ static void launch_fwd_impl(PlanTable& pt, const TileDesc* tiles, const int2* it
   if (nitems == 0) return;
   if (MASK || !launch_fwd_fixed(tx, ty, threads > 0 ? threads : kThreads, pt, tiles, items, nitems, smem, spec, g,
                                 s)) {
+    EpiBoxes src;
+    std::memset(&src, 0, sizeof(src));
+    src.count = !MASK && use_l2_prefetch() &&
+                volume_box_map(g.v.data, g.v.nx, g.v.ny, g.v.nz, tma_box_width(tx), ty, &src.map[0]);
     auto k = plane_fwd_kernel<Gather, MASK>;
     set_smem(k, smem);
-    k<<<nitems, threads > 0 ? threads : kThreads, smem, s>>>(tiles, items, pt.device(), spec, g);
+    k<<<nitems, threads > 0 ? threads : kThreads, smem, s>>>(tiles, items, pt.device(), spec, g, src, resident_ctas());
   }
   MVD_CHECK(cudaGetLastError());
   count_launch();

@@ -58,7 +58,7 @@ static void launch_inv_impl(PlanTable& pt, const ConvPlan& p, const float2* spec
     set_smem(k, p.smem_plane);
     const int threads = p.threads_plane > 0 ? p.threads_plane : kThreads;
     k<<<nitems, threads, p.smem_plane, s>>>(p.d_tiles.as<TileDesc>(), p.d_items_inv.as<int2>(), pt.device(), spec,
-                                            e);
+                                            e, epilogue_boxes(p, e));
   }
   MVD_CHECK(cudaGetLastError());
   count_launch();
@@ -94,7 +94,7 @@ void launch_inv_store_items(PlanTable& pt, const ConvPlan& p, const TileDesc* ti
     auto k = plane_inv_kernel<EpiStore>;
     set_smem(k, p.smem_plane);
     k<<<nitems, p.threads_plane > 0 ? p.threads_plane : kThreads, p.smem_plane, s>>>(tiles, items, pt.device(), spec,
-                                                                                     EpiStore{out, nx, ny});
+                                                                                     EpiStore{out, nx, ny}, EpiBoxes{});
   }
   MVD_CHECK(cudaGetLastError());
   count_launch();
