@@ -325,6 +325,25 @@ bool volume_box_map(const float* base, int nx, int ny, int nz, int w, int h, CUt
 }
 
 
+bool use_l2_prefetch() {
+  static bool on = [] {
+    const char* e = std::getenv("MVD_L2_PREFETCH");
+    return !(e && e[0] == '0');
+  }();
+  return on;
+}
+
+// The slice-copy forward kernel is opt-in (MVD_TMA=1): with one slice per CTA the copy's latency
+// stands in front of all of the CTA's work, and on cfg2 it measured slower (0.735 vs 0.62 ms of
+// forward passes per iteration) than the gather that keeps ~20 loads per thread in flight.
+bool use_tma() {
+  static bool on = [] {
+    const char* e = std::getenv("MVD_TMA");
+    return e && e[0] == '1';
+  }();
+  return on;
+}
+
 bool use_fixed_planes() {
   static bool on = [] {
     const char* e = std::getenv("MVD_FIXED_PLANES");

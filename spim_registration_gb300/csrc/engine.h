@@ -136,7 +136,12 @@ int plane_threads();
 // Whether compiled tile shapes use their compile-time-shaped plane kernels (MVD_FIXED_PLANES=0
 // selects the generic kernels everywhere).
 bool use_fixed_planes();
-// Slice copies of the forward plane pass whose bounded wait gave up on the current device.
+// L2 prefetch through tensor maps in the plane kernels (MVD_L2_PREFETCH=0 turns it off).
+bool use_l2_prefetch();
+// The TMA slice-copy forward kernel for compiled shapes (opt-in: MVD_TMA=1).
+bool use_tma();
+// Slice copies of the forward plane pass whose bounded wait gave up on the current device since
+// the last call (the counter is reset); 0 when the slice-copy kernel is off.
 int tma_timeouts();
 // Tensor map of a float volume [nz][ny][nx] with a (w, h, 1) box (cached); false when the volume
 // does not meet the tensor copy's rules (16-byte aligned base and row stride, box <= 256).

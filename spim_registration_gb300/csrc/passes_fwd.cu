@@ -16,28 +16,12 @@ namespace mvd {
 
 namespace {
 
-bool use_l2_prefetch() {
-  static bool on = [] {
-    const char* e = std::getenv("MVD_L2_PREFETCH");
-    return !(e && e[0] == '0');
-  }();
-  return on;
-}
-
 // CTAs of a plane kernel resident at once on the current device (two per SM)
 int resident_ctas() {
   int dev = 0, sms = 0;
   MVD_CHECK(cudaGetDevice(&dev));
   MVD_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   return 2 * sms;
-}
-
-bool use_tma() {
-  static bool on = [] {
-    const char* e = std::getenv("MVD_TMA");
-    return e && e[0] == '1';
-  }();
-  return on;
 }
 
 // Per-device count of slice copies whose wait gave up (zero unless a copy never completed).
@@ -58,8 +42,10 @@ int* tma_timeout_counter() {
 }  // namespace
 
 int tma_timeouts() {
+  if (!use_tma()) return 0;
   int n = 0;
   MVD_CHECK(cudaMemcpy(&n, tma_timeout_counter(), sizeof(int), cudaMemcpyDeviceToHost));
+  if (n) MVD_CHECK(cudaMemset(tma_timeout_counter(), 0, sizeof(int)));
   return n;
 }
 

@@ -7,14 +7,6 @@
 
 namespace mvd {
 
-static bool use_l2_prefetch() {
-  static bool on = [] {
-    const char* e = std::getenv("MVD_L2_PREFETCH");
-    return !(e && e[0] == '0');
-  }();
-  return on;
-}
-
 // Tensor maps for the L2 prefetch of the volumes the epilogue reads (none if any is refused).
 template <class Epi>
 static EpiBoxes epilogue_boxes(const ConvPlan& p, const Epi& e) {
