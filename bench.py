@@ -359,7 +359,9 @@ def run_inputs(prob, device, hbm_peak, reps=5):
     fused box's size, rotated about y by 180 v / V degrees with a fractional shift) resampled
     with its blending weight, the overlap statistics and the VIRTUAL normalisation with the
     average-overlap OSEM factor.  Algorithmic bytes: resample 4 (view) + 8 (image, weight)
-    per voxel and view; overlap 4 per voxel and view; normalisation 8 per voxel and view."""
+    per voxel and view; overlap 4 per voxel and view; normalisation 8 per voxel and view.
+    The resample and normalisation launches queue behind a short device-side sleep, so their
+    events time the kernels, not the host's launch overhead."""
     import math
 
     import torch
@@ -378,21 +380,24 @@ def run_inputs(prob, device, hbm_peak, reps=5):
         shift = (cx - (c * cx + s_ * cz) + 0.25, 0.375, cz - (-s_ * cx + c * cz) + 0.125)
         affines.append([c, 0, s_, shift[0], 0, 1, 0, shift[1], -s_, 0, c, shift[2]])
     border, blend = (0.0, 0.0, 0.0), (20.0, 20.0, 20.0)
-    ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(5)]
     ms = np.zeros(3)
     for r in range(reps + 1):
         torch.cuda.synchronize()
+        torch.cuda._sleep(4_000_000)  # about 2 ms: the host queues the launches meanwhile
         ev[0].record()
         outs = [transform_input(raw[v], affines[v], (0, 0, 0), (nz, ny, nx), border, blend, device) for v in range(V)]
         ev[1].record()
         wn = WeightNormalizer([o[1] for o in outs], num_portions=32)
         wn.process()  # waits for the stream: returns the statistics to the host
         ev[2].record()
-        wn.apply(wn.osem_speedup(2))
+        torch.cuda._sleep(1_000_000)
         ev[3].record()
+        wn.apply(wn.osem_speedup(2))
+        ev[4].record()
         torch.cuda.synchronize()
         if r:
-            ms += [ev[0].elapsed_time(ev[1]), ev[1].elapsed_time(ev[2]), ev[2].elapsed_time(ev[3])]
+            ms += [ev[0].elapsed_time(ev[1]), ev[1].elapsed_time(ev[2]), ev[3].elapsed_time(ev[4])]
         del outs, wn
     ms /= reps
     algo = [12.0 * n * V, 4.0 * n * V, 8.0 * n * V]

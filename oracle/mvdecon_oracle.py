@@ -498,7 +498,19 @@ def transform_input(view, affine_rows, offset_xyz, out_shape_zyx):
     return np.where(inside, np.maximum(float(MIN_VALUE), out), 0.0)
 
 
-_BLEND_LUT = np.array([(math.cos((1 - k / 1000.0) * math.pi) + 1) / 2 for k in range(1001)])
+def _blend_lut():
+    """The lookup table as BlendingRealRandomAccess's static block fills it (:47-53): d steps by
+    0.001 in double from 0 while d <= 1.0001, and entry round(d * 1000) holds the value at the
+    accumulated d (which drifts from k / 1000 in the last bits)."""
+    lut = np.zeros(1001)
+    d = 0.0
+    while d <= 1.0001:
+        lut[int(math.floor(d * 1000.0 + 0.5))] = (math.cos((1 - d) * math.pi) + 1) / 2
+        d = d + 0.001
+    return lut
+
+
+_BLEND_LUT = _blend_lut()
 
 
 def transform_weights(view_shape_zyx, affine_rows, offset_xyz, out_shape_zyx, border_xyz, blending_xyz):

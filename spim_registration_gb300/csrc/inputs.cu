@@ -6,9 +6,12 @@
 //   WeightNormalizer (VIRTUAL)  spim/process/fusion/deconvolution/WeightNormalizer.java:73-253,
 //                               spim/process/fusion/weights/NormalizingRandomAccess.java:57-66
 //   OSEM factor                 ProcessForDeconvolution.java:372-405
+#include <climits>
 #include <cmath>
 #include <cstring>
+#include <stdexcept>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "../../include/mvdecon.h"
@@ -26,8 +29,12 @@ struct Affine {  // world -> view (the inverse of the view's registration), row-
   float m[12];
 };
 
-// BlendingRealRandomAccess's 1001-entry lookup table of (cos((1 - d) pi) + 1) / 2
-__constant__ double c_blend_lut[1001];
+// BlendingRealRandomAccess's 1001-entry lookup table of (cos((1 - d) pi) + 1) / 2, in global
+// memory read through L1 (each thread looks up its own entry, which the constant cache would
+// serialise across a warp): as doubles, and as float pairs hi + lo with hi = (float)L and
+// lo = (float)(L - hi), within 2^-48 relative of the double L
+__device__ double g_blend_lut[1001];
+__device__ float2 g_blend_pair[1001];
 
 __device__ __forceinline__ int mirror_single_i(int i, int n) {
   if (i >= 0 && i < n) return i;
@@ -38,7 +45,9 @@ __device__ __forceinline__ int mirror_single_i(int i, int n) {
   return m < n ? m : period - m;
 }
 
-// NLinearInterpolator over Views.extendMirrorSingle(img) at the real position t
+// NLinearInterpolator over Views.extendMirrorSingle(img) at the real position t; Index is the
+// voxel index type (32-bit when the view holds fewer than 2^31 voxels)
+template <class Index>
 __device__ __forceinline__ float trilinear_mirror(const float* __restrict__ img, int sx, int sy, int sz, float tx,
                                                   float ty, float tz) {
   const float fx0 = floorf(tx), fy0 = floorf(ty), fz0 = floorf(tz);
@@ -52,64 +61,10 @@ __device__ __forceinline__ float trilinear_mirror(const float* __restrict__ img,
   for (int c = 0; c < 8; ++c) {
     const int bx = c & 1, by = (c >> 1) & 1, bz = (c >> 2) & 1;
     const float w = (bx ? ax : 1.f - ax) * (by ? ay : 1.f - ay) * (bz ? az : 1.f - az);
-    acc += w * __ldg(img + ((long long)zs[bz] * sy + ys[by]) * sx + xs[bx]);
+    acc += w * __ldg(img + ((Index)zs[bz] * sy + ys[by]) * sx + xs[bx]);
   }
   return acc;
 }
-
-// BlendingRealRandomAccess.computeWeight (:91-121) on the view interval [0, size)
-__device__ __forceinline__ float blend_weight(float lx, float ly, float lz, int sx, int sy, int sz, float3 border,
-                                              float3 range) {
-  const float loc[3] = {lx, ly, lz};
-  const float dm1[3] = {(float)(sx - 1), (float)(sy - 1), (float)(sz - 1)};
-  const float b[3] = {border.x, border.y, border.z};
-  const float r[3] = {range.x, range.y, range.z};
-  float w = 1.f;
-#pragma unroll
-  for (int d = 0; d < 3; ++d) {
-    const float l = loc[d];
-    const float dist = fmaxf(0.f, fminf(l - b[d], dm1[d] - l - b[d]));
-    if (dist == 0.f) return 0.f;
-    const float rel = dist / r[d];
-    if (rel < 1.f) {
-      // indexFor(d) = Math.round(d * 1000.0)
-      const int idx = (int)floor((double)rel * 1000.0 + 0.5);
-      w = (float)((double)w * c_blend_lut[idx]);
-    }
-  }
-  return w;
-}
-
-// One thread per output voxel; a block covers a 32 x 8 patch of one z plane, so its view
-// positions stay close together whatever the rotation (the view's reads hit L1/L2).
-__global__ void __launch_bounds__(256) transform_view_kernel(const float* __restrict__ view, int sx, int sy, int sz,
-                                                             Affine inv, int ox, int oy, int oz, int nx, int ny,
-                                                             float* __restrict__ out_img,
-                                                             float* __restrict__ out_blend, float3 border,
-                                                             float3 range) {
-  const int x = blockIdx.x * 32 + threadIdx.x, y = blockIdx.y * 8 + threadIdx.y, z = blockIdx.z;
-  if (x >= nx || y >= ny) return;
-  const long long i = ((long long)z * ny + y) * nx + x;
-  const float s0 = (float)(x + ox), s1 = (float)(y + oy), s2 = (float)(z + oz);
-  const float t0 = inv.m[0] * s0 + inv.m[1] * s1 + inv.m[2] * s2 + inv.m[3];
-  const float t1 = inv.m[4] * s0 + inv.m[5] * s1 + inv.m[6] * s2 + inv.m[7];
-  const float t2 = inv.m[8] * s0 + inv.m[9] * s1 + inv.m[10] * s2 + inv.m[11];
-  if (out_img) {
-    float v = 0.f;  // no image data (MVDeconvolution.computeQuotient reads 0 as "no data")
-    if (t0 >= 0.f && t1 >= 0.f && t2 >= 0.f && t0 < (float)sx && t1 < (float)sy && t2 < (float)sz)
-      v = fmaxf(1e-4f, trilinear_mirror(view, sx, sy, sz, t0, t1, t2));
-    out_img[i] = v;
-  }
-  // the blending weight is defined everywhere (the border can be negative)
-  if (out_blend) out_blend[i] = blend_weight(t0, t1, t2, sx, sy, sz, border, range);
-}
-
-struct WeightPtrs {
-  float* p[16];
-};
-
-// Math.min(1, x) of the reference: NaN stays NaN (fminf would return 1)
-__device__ __forceinline__ float java_min1(float x) { return x != x ? x : fminf(1.f, x); }
 
 // The reference normalises in double; GB300's FP64 pipe is a small fraction of its FP32 one.
 // The sum over the views stays in double (the reference's sequential double sum cannot be
@@ -127,17 +82,25 @@ struct FF {  // hi + lo
   float hi, lo;
 };
 
-// y = the float nearest hi + lo; false when that rounding is not certain
+// y = the float nearest hi + lo; false when that rounding is not certain.  The pair must come
+// from error-free steps on operands whose products did not underflow (nonzero operands of at
+// least 2^-96, see tiny()); a zero pair is then an exact zero, and lo == 0 an exact hi.
 __device__ __forceinline__ bool round_pair(FF x, float& y) {
   y = __fadd_rn(x.hi, x.lo);
-  if (x.lo == 0.f) return true;
+  if (x.hi == 0.f && x.lo == 0.f) return true;
   const unsigned b = __float_as_uint(y);
   const unsigned ex = b & 0x7f800000u;
-  if (ex <= (24u << 23) || ex == 0x7f800000u || (b & 0x007fffffu) == 0u) return false;
+  if (ex <= (24u << 23) || ex == 0x7f800000u) return false;  // below 2^-102, infinite or NaN
+  if (x.lo == 0.f) return true;
+  if ((b & 0x007fffffu) == 0u) return false;  // a power of two: the half ulp below is smaller
   const float half_ulp = __uint_as_float(ex - (24u << 23));
   const float d = __fadd_rn(__fsub_rn(x.hi, y), x.lo);  // (hi + lo) - y; hi - y is exact
   return fabsf(d) < __fmul_rn(half_ulp, 0.99993896484375f);
 }
+
+// nonzero and below 2^-96: too small for the error-free steps (their error terms could
+// underflow)
+__device__ __forceinline__ bool tiny(float x) { return x != 0.f && (__float_as_uint(x) & 0x7f800000u) < (31u << 23); }
 
 // w / (d.hi + d.lo) as a pair: q = fl(w / d.hi) is correctly rounded, so w - q d.hi is exact
 // (an FMA); the remainder over d gives the low part.
@@ -153,6 +116,79 @@ __device__ __forceinline__ FF ff_mul(FF a, FF b) {
   const float e = __fmaf_rn(a.hi, b.hi, -p);
   return {p, __fadd_rn(e, __fadd_rn(__fmul_rn(a.hi, b.lo), __fmul_rn(a.lo, b.hi)))};
 }
+
+// BlendingRealRandomAccess.computeWeight (:91-121) on the view interval [0, size)
+__device__ __forceinline__ float blend_weight(float lx, float ly, float lz, int sx, int sy, int sz, float3 border,
+                                              float3 range) {
+  const float loc[3] = {lx, ly, lz};
+  const float dm1[3] = {(float)(sx - 1), (float)(sy - 1), (float)(sz - 1)};
+  const float b[3] = {border.x, border.y, border.z};
+  const float r[3] = {range.x, range.y, range.z};
+  float w = 1.f;
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    const float l = loc[d];
+    const float dist = fmaxf(0.f, fminf(l - b[d], dm1[d] - l - b[d]));
+    if (dist == 0.f) return 0.f;
+    // relDist = dist / blending, multiplied in only when below 1: dist >= blending makes the
+    // quotient at least 1, so the division is needed only below the blending distance
+    if (!(dist >= r[d])) {
+      const float rel = dist / r[d];
+      if (!(rel < 1.f)) continue;
+      // indexFor(d) = Math.round(d * 1000.0): the double product of a float and 1000 is exact,
+      // so the index is the exact round-half-up of rel * 1000, found in float by two FMA sign
+      // tests around a first guess (each FMA rounds once, which keeps the sign)
+      int idx = __float2int_rd(__fmaf_rn(rel, 1000.f, 0.5f));
+      if (__fmaf_rn(rel, 1000.f, 0.5f - (float)idx) < 0.f)
+        --idx;
+      else if (__fmaf_rn(rel, 1000.f, -0.5f - (float)idx) >= 0.f)
+        ++idx;
+      idx = min(max(idx, 0), 1000);
+      // minDistance *= lookUp[idx]: the float nearest the double-rounded double product,
+      // certified from the float pair (the double rounding cannot move a product that lies
+      // farther than 2^-14 half ulps from a float rounding boundary), else in double
+      const float2 L = __ldg(g_blend_pair + idx);
+      float y;
+      if (round_pair(ff_mul(FF{w, 0.f}, FF{L.x, L.y}), y))
+        w = y;
+      else
+        w = (float)((double)w * __ldg(g_blend_lut + idx));
+    }
+  }
+  return w;
+}
+
+// One thread per output voxel; a block covers a 32 x 8 patch of one z plane, so its view
+// positions stay close together whatever the rotation (the view's reads hit L1/L2).
+template <class Index>
+__global__ void __launch_bounds__(256) transform_view_kernel(const float* __restrict__ view, int sx, int sy, int sz,
+                                                             Affine inv, int ox, int oy, int oz, int nx, int ny,
+                                                             float* __restrict__ out_img,
+                                                             float* __restrict__ out_blend, float3 border,
+                                                             float3 range) {
+  const int x = blockIdx.x * 32 + threadIdx.x, y = blockIdx.y * 8 + threadIdx.y, z = blockIdx.z;
+  if (x >= nx || y >= ny) return;
+  const long long i = ((long long)z * ny + y) * nx + x;
+  const float s0 = (float)(x + ox), s1 = (float)(y + oy), s2 = (float)(z + oz);
+  const float t0 = inv.m[0] * s0 + inv.m[1] * s1 + inv.m[2] * s2 + inv.m[3];
+  const float t1 = inv.m[4] * s0 + inv.m[5] * s1 + inv.m[6] * s2 + inv.m[7];
+  const float t2 = inv.m[8] * s0 + inv.m[9] * s1 + inv.m[10] * s2 + inv.m[11];
+  if (out_img) {
+    float v = 0.f;  // no image data (MVDeconvolution.computeQuotient reads 0 as "no data")
+    if (t0 >= 0.f && t1 >= 0.f && t2 >= 0.f && t0 < (float)sx && t1 < (float)sy && t2 < (float)sz)
+      v = fmaxf(1e-4f, trilinear_mirror<Index>(view, sx, sy, sz, t0, t1, t2));
+    out_img[i] = v;
+  }
+  // the blending weight is defined everywhere (the border can be negative)
+  if (out_blend) out_blend[i] = blend_weight(t0, t1, t2, sx, sy, sz, border, range);
+}
+
+struct WeightPtrs {
+  float* p[16];
+};
+
+// Math.min(1, x) of the reference: NaN stays NaN (fminf would return 1)
+__device__ __forceinline__ float java_min1(float x) { return x != x ? x : fminf(1.f, x); }
 
 // One voxel with the reference's own double arithmetic; the weights are read again from
 // memory, which the certified pass has not written for this voxel.
@@ -176,6 +212,78 @@ __device__ __forceinline__ void normalize_voxel_double(const WeightPtrs& w, int 
     }
 }
 
+// k >= 0 rounded to `bits` significant bits, to nearest with ties to even
+__device__ __forceinline__ long long round_sig(long long k, int bits) {
+  const int nb = 64 - __clzll(k);
+  if (nb <= bits) return k;
+  const int sh = nb - bits;
+  const long long low = k & ((1LL << sh) - 1), half = 1LL << (sh - 1);
+  k -= low;
+  if (low > half || (low == half && ((k >> sh) & 1))) k += 1LL << sh;
+  return k;
+}
+
+// k * 2^e rounded once to float (|k| < 2^62), in integer operations only (a 64-bit integer
+// conversion would take the FP64 pipe); false when the result is not a normal float
+__device__ __forceinline__ bool scaled_float(long long k, int e, float& out) {
+  if (k == 0) {
+    out = 0.f;
+    return true;
+  }
+  const unsigned sign = k < 0 ? 0x80000000u : 0u;
+  const long long a = round_sig(k < 0 ? -k : k, 24);
+  const int nb = 64 - __clzll(a);  // a = m 2^(nb - 24), m in [2^23, 2^24)
+  const unsigned m = nb >= 24 ? (unsigned)(a >> (nb - 24)) : (unsigned)a << (24 - nb);
+  const int ex = nb - 1 + e + 127;
+  if (ex < 1 || ex > 254) return false;
+  out = __uint_as_float(sign | ((unsigned)ex << 23) | (m & 0x7fffffu));
+  return true;
+}
+
+// The reference's sequential double sum of the views' weights (0.0 + w_0 + w_1 + ...), as
+// the float pair hi = (float)sum, lo = (float)(sum - hi), without FP64 arithmetic (GB300's FP64
+// pipe would bound the kernel).  A positive float is m 2^s with a 24-bit integer m; aligned on
+// the smallest s of the nonzero weights, every partial sum is an integer K, and the double
+// addition's rounding is K rounded to 53 significant bits (ties to even), so the integers
+// follow the double sum exactly.  false when that is not certain: a negative, infinite or NaN
+// weight, exponents spread over more than 34 binades (the aligned sum would overflow 63 bits),
+// or a result outside the normal float range; the caller then sums in double.
+__device__ __forceinline__ bool exact_view_sum(const float* wv, int nv, float& hi, float& lo) {
+  int emin = 1 << 20, emax = -(1 << 20);
+#pragma unroll
+  for (int v = 0; v < 16; ++v)
+    if (v < nv) {
+      const unsigned b = __float_as_uint(wv[v]);
+      if (b & 0x80000000u) {
+        if (b != 0x80000000u) return false;  // negative (-0 adds nothing)
+        continue;
+      }
+      const int be = (int)(b >> 23);
+      if (be == 255) return false;
+      if (b == 0) continue;
+      const int sv = (be ? be : 1) - 150;
+      emin = min(emin, sv);
+      emax = max(emax, sv);
+    }
+  if (emax < emin) {  // every weight zero
+    hi = lo = 0.f;
+    return true;
+  }
+  if (emax - emin > 34) return false;
+  long long k = 0;
+#pragma unroll
+  for (int v = 0; v < 16; ++v)
+    if (v < nv) {
+      const unsigned b = __float_as_uint(wv[v]);
+      if (b == 0u || b == 0x80000000u) continue;
+      const int be = (int)(b >> 23);
+      const long long m = (long long)((b & 0x7fffffu) | (be ? 0x800000u : 0u));
+      k = round_sig(k + (m << (((be ? be : 1) - 150) - emin)), 53);
+    }
+  const long long khi = round_sig(k, 24);
+  return scaled_float(khi, emin, hi) && scaled_float(k - khi, emin, lo);
+}
+
 struct Deferred {  // voxels left to the double pass
   long long* list;
   unsigned long long* count;
@@ -190,8 +298,12 @@ struct Deferred {  // voxels left to the double pass
 // (float)(w_v / sum_w) with no guard on the sum (0 / 0 gives NaN where no view has weight, as
 // in the reference), then min(1, w * (float)osem) in float.
 // osem arrives as a float pair too (osem_hi + osem_lo == osem to ~48 bits).
-__global__ void normalize_weights_kernel(WeightPtrs w, int nv, long long n, double osem, float osem_hi,
-                                         float osem_lo, int mode, Deferred def) {
+// The view count is a template parameter: guards on a runtime count would still issue the
+// instructions of all 16 view slots.
+template <int NV>
+__global__ void normalize_weights_kernel(WeightPtrs w, long long n, double osem, float osem_hi, float osem_lo,
+                                         int mode, Deferred def) {
+  constexpr int nv = NV;
   const FF os = {osem_hi, osem_lo};
   const bool unit = osem == 1.0;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
@@ -199,13 +311,19 @@ __global__ void normalize_weights_kernel(WeightPtrs w, int nv, long long n, doub
 #pragma unroll
     for (int v = 0; v < 16; ++v)
       if (v < nv) wv[v] = w.p[v][i];
-    double sum_d = 0.0;
+    float s_hi, s_lo;  // (float)sum_w and (float)(sum_w - s_hi)
+    if (!exact_view_sum(wv, nv, s_hi, s_lo)) {
+      double sum_d = 0.0;
 #pragma unroll
-    for (int v = 0; v < 16; ++v)
-      if (v < nv) sum_d += (double)wv[v];
+      for (int v = 0; v < 16; ++v)
+        if (v < nv) sum_d += (double)wv[v];
+      s_hi = (float)sum_d;
+      s_lo = (float)(sum_d - (double)s_hi);
+    }
     bool certain = true;
     if (mode == 0) {
-      const float norm = sum_d > 1.0 ? (float)sum_d : 1.f;
+      // sum_w > 1 ? (float)sum_w : 1, NaN included (a NaN sum gives 1)
+      const float norm = fmaxf(s_hi, 1.f);
 #pragma unroll
       for (int v = 0; v < 16; ++v)
         if (v < nv) {
@@ -213,21 +331,21 @@ __global__ void normalize_weights_kernel(WeightPtrs w, int nv, long long n, doub
           if (unit) {
             y = __fdiv_rn(wv[v], norm);
           } else {
-            certain = round_pair(ff_mul(ff_quotient(wv[v], FF{norm, 0.f}), os), y) && certain;
+            const FF q = ff_quotient(wv[v], FF{norm, 0.f});
+            certain = !tiny(wv[v]) && !tiny(q.hi) && round_pair(ff_mul(q, os), y) && certain;
           }
           out[v] = java_min1(y);
         }
     } else {
-      const float s_hi = (float)sum_d;
-      const FF sum = {s_hi, (float)(sum_d - (double)s_hi)};
+      const FF sum = {s_hi, s_lo};
 #pragma unroll
       for (int v = 0; v < 16; ++v)
         if (v < nv) {
           float x = 0.f;
-          if (sum_d == 0.0) {
+          if (s_hi == 0.f) {  // a sum of floats is 0 or at least 2^-149 in magnitude
             x = __fdiv_rn(wv[v], 0.f);  // w / 0: NaN (0 / 0) or an infinity, as in double
           } else {
-            certain = round_pair(ff_quotient(wv[v], sum), x) && certain;
+            certain = !tiny(wv[v]) && !tiny(s_hi) && round_pair(ff_quotient(wv[v], sum), x) && certain;
           }
           out[v] = java_min1(__fmul_rn(x, osem_hi));  // (float)osemspeedup: the float osem
         }
@@ -265,16 +383,22 @@ __global__ void normalize_deferred_kernel(WeightPtrs w, int nv, double osem, int
 // FusionHelper.divideIntoPortions(n, P), the sum of the counts.  Each block walks one
 // contiguous range, so a warp's 32 voxels lie in one portion except at the few portion
 // borders; lane 0 keeps the running sum of its portion in a register.
-__global__ void weight_overlap_kernel(WeightPtrs w, int nv, long long n, long long chunk, int portions,
-                                      long long span, unsigned long long* __restrict__ portion_sum,
-                                      int* __restrict__ min_count) {
+template <int NV>
+__global__ void weight_overlap_kernel(WeightPtrs w, long long n, long long chunk, int portions, long long span,
+                                      unsigned long long* __restrict__ portion_sum, int* __restrict__ min_count) {
+  constexpr int nv = NV;
   const long long lo = blockIdx.x * span;
   const long long hi = lo + span < n ? lo + span : n;
   const int lane = threadIdx.x & 31;
   int local_min = nv;
   int cur = -1;
   unsigned long long acc = 0;
-  for (long long base = lo + (threadIdx.x & ~31); base < hi; base += blockDim.x) {
+  // portion of i = min(P - 1, i / chunk), followed incrementally from one 64-bit division:
+  // p0 is the portion of the warp's first voxel, [p0 chunk, bnd) its range
+  const long long first = lo + (threadIdx.x & ~31);
+  int p0 = first < hi ? (int)min((long long)portions - 1, first / chunk) : 0;
+  long long bnd = p0 == portions - 1 ? LLONG_MAX : (long long)(p0 + 1) * chunk;
+  for (long long base = first; base < hi; base += blockDim.x) {
     const long long i = base + lane;
     int c = 0;
     if (i < hi) {
@@ -283,10 +407,12 @@ __global__ void weight_overlap_kernel(WeightPtrs w, int nv, long long n, long lo
         if (v < nv) c += w.p[v][i] > 0.f;
       local_min = min(local_min, c);
     }
+    while (base >= bnd) {
+      ++p0;
+      bnd = p0 == portions - 1 ? LLONG_MAX : bnd + chunk;
+    }
     const long long last = (base + 31 < hi ? base + 31 : hi - 1);
-    const int p0 = (int)min((long long)portions - 1, base / chunk);
-    const int p1 = (int)min((long long)portions - 1, last / chunk);
-    if (p0 == p1) {
+    if (last < bnd) {
       const unsigned s = __reduce_add_sync(0xffffffffu, (unsigned)c);
       if (lane == 0) {
         if (p0 != cur) {
@@ -297,12 +423,34 @@ __global__ void weight_overlap_kernel(WeightPtrs w, int nv, long long n, long lo
         acc += s;
       }
     } else if (i < hi && c) {
-      atomicAdd(portion_sum + (int)min((long long)portions - 1, i / chunk), (unsigned long long)c);
+      int p = p0;
+      for (long long b = bnd; i >= b;) {  // the warp spans at most 32 voxels
+        ++p;
+        b = p == portions - 1 ? LLONG_MAX : b + chunk;
+      }
+      atomicAdd(portion_sum + p, (unsigned long long)c);
     }
   }
   if (lane == 0 && cur >= 0 && acc) atomicAdd(portion_sum + cur, acc);
   const int m = __reduce_min_sync(0xffffffffu, local_min);
   if (lane == 0) atomicMin(min_count, m);
+}
+
+// f(std::integral_constant<int, nv>{}) for a view count 1..16
+template <class F>
+void with_view_count(int nv, F&& f) {
+  switch (nv) {
+#define MVD_NV_CASE(N) \
+  case N:              \
+    f(std::integral_constant<int, N>{}); \
+    break;
+    MVD_NV_CASE(1) MVD_NV_CASE(2) MVD_NV_CASE(3) MVD_NV_CASE(4) MVD_NV_CASE(5) MVD_NV_CASE(6) MVD_NV_CASE(7)
+    MVD_NV_CASE(8) MVD_NV_CASE(9) MVD_NV_CASE(10) MVD_NV_CASE(11) MVD_NV_CASE(12) MVD_NV_CASE(13)
+    MVD_NV_CASE(14) MVD_NV_CASE(15) MVD_NV_CASE(16)
+#undef MVD_NV_CASE
+    default:
+      throw std::invalid_argument("1..16 views");
+  }
 }
 
 int grid_n(long long n) {
@@ -314,11 +462,18 @@ bool g_lut_ready[64] = {};
 
 void upload_lut(int dev) {
   if (dev < 64 && g_lut_ready[dev]) return;
-  double lut[1001];
-  // the reference fills the table by stepping d in 0.001 increments; index k holds the value
-  // of d = k / 1000 (to within the accumulated rounding of the step)
-  for (int k = 0; k <= 1000; ++k) lut[k] = (std::cos((1.0 - k / 1000.0) * M_PI) + 1.0) / 2.0;
-  MVD_CHECK(cudaMemcpyToSymbol(c_blend_lut, lut, sizeof(lut)));
+  double lut[1001] = {};
+  float2 pair[1001];
+  // the reference's static block: d steps by 0.001 in double from 0 while d <= 1.0001, and
+  // entry round(d * 1000) holds the value at the accumulated d (not exactly k / 1000)
+  for (double d = 0; d <= 1.0001; d = d + 0.001)
+    lut[(int)std::floor(d * 1000.0 + 0.5)] = (std::cos((1 - d) * M_PI) + 1) / 2;
+  for (int k = 0; k <= 1000; ++k) {
+    const float hi = (float)lut[k];
+    pair[k] = make_float2(hi, (float)(lut[k] - (double)hi));
+  }
+  MVD_CHECK(cudaMemcpyToSymbol(g_blend_lut, lut, sizeof(lut)));
+  MVD_CHECK(cudaMemcpyToSymbol(g_blend_pair, pair, sizeof(pair)));
   if (dev < 64) g_lut_ready[dev] = true;
 }
 
@@ -384,7 +539,9 @@ extern "C" int mvd_transform_view(const float* view, const int* vd, const double
       return MVD_ERR_ARG;
     }
     const dim3 grid((od[0] + 31) / 32, (od[1] + 7) / 8, od[2]);
-    transform_view_kernel<<<grid, dim3(32, 8), 0, static_cast<cudaStream_t>(stream)>>>(
+    const bool narrow = (long long)vd[0] * vd[1] * vd[2] < (1LL << 31);
+    (narrow ? transform_view_kernel<int> : transform_view_kernel<long long>)<<<grid, dim3(32, 8), 0,
+                                                                              static_cast<cudaStream_t>(stream)>>>(
         view, vd[0], vd[1], vd[2], inv, offset[0], offset[1], offset[2], od[0], od[1], out_img, out_blend, b, r);
     MVD_CHECK(cudaGetLastError());
     count_launch();
@@ -427,7 +584,9 @@ extern "C" int mvd_normalize_weights(float* const* weights, int num_views, long 
     def.count = static_cast<unsigned long long*>(buf);
     def.list = reinterpret_cast<long long*>(def.count + 1);
     MVD_CHECK(cudaMemsetAsync(def.count, 0, sizeof(unsigned long long), s));
-    normalize_weights_kernel<<<grid_n(n), 256, 0, s>>>(wp, num_views, n, osem, osem_hi, osem_lo, mode, def);
+    with_view_count(num_views, [&](auto nv) {
+      normalize_weights_kernel<decltype(nv)::value><<<grid_n(n), 256, 0, s>>>(wp, n, osem, osem_hi, osem_lo, mode, def);
+    });
     MVD_CHECK(cudaGetLastError());
     count_launch();
     normalize_deferred_kernel<<<152 * 4, 256, 0, s>>>(wp, num_views, osem, mode, def);
@@ -475,7 +634,9 @@ extern "C" int mvd_weight_overlap(const float* const* weights, int num_views, lo
     long long span = (n + grid - 1) / grid;
     span = (span + 31) / 32 * 32;
     const long long chunk = n / num_portions;
-    weight_overlap_kernel<<<grid, 256, 0, s>>>(wp, num_views, n, chunk, num_portions, span, d_sum, d_min);
+    with_view_count(num_views, [&](auto nv) {
+      weight_overlap_kernel<decltype(nv)::value><<<grid, 256, 0, s>>>(wp, n, chunk, num_portions, span, d_sum, d_min);
+    });
     MVD_CHECK(cudaGetLastError());
     count_launch();
     std::vector<unsigned long long> sums(num_portions);

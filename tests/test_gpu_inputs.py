@@ -63,12 +63,60 @@ def test_transform_view_matches_oracle(angle, scale):
     assert np.mean(gb == wb) > 0.98
 
 
+def _blend_on_device(lib, torch, view_zyx, out_zyx, border, blend, offset=(0, 0, 0)):
+    eye = [1.0, 0, 0, 0, 0, 1.0, 0, 0, 0, 0, 1.0, 0]
+    dv = torch.ones(view_zyx, dtype=torch.float32, device="cuda")
+    oblend = torch.full(out_zyx, float("nan"), device="cuda")
+    vz, vy, vx = view_zyx
+    oz, oy, ox = out_zyx
+    native.check(lib.mvd_transform_view(dv.data_ptr(), native.iarr([vx, vy, vz]), (native.ctypes.c_double * 12)(*eye),
+                                        native.iarr(list(offset)), native.iarr([ox, oy, oz]), None,
+                                        oblend.data_ptr(), (native.ctypes.c_float * 3)(*border),
+                                        (native.ctypes.c_float * 3)(*blend), 0, None))
+    torch.cuda.synchronize()
+    return oblend.cpu().numpy()
+
+
+def test_blending_weight_arithmetic_is_bit_exact():
+    """With the identity registration the kernel and the oracle see the same float positions,
+    so the weights must agree bit for bit: the lookup index (Math.round of the double product
+    rel * 1000) and minDistance *= lookUp[i] (float times double, rounded twice) over products
+    of two and three table entries, with fractional borders and blending ranges."""
+    torch = pytest.importorskip("torch")
+    lib = native.load()
+    view, border, blend = (61, 70, 83), (0.3, -1.7, 2.1), (40.3, 35.7, 30.1)
+    got = _blend_on_device(lib, torch, view, view, border, blend)
+    want = O.transform_weights(view, [1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0], (0, 0, 0), view, border, blend)
+    assert (want > 0).mean() > 0.8 and len(np.unique(want)) > 10000
+    np.testing.assert_array_equal(got, want)
+
+
+def test_blending_lookup_index_at_half_steps():
+    """rel = (x - 0.5) / 1000: every rel * 1000 lies within a float rounding of k + 0.5, the
+    boundary between two table entries."""
+    torch = pytest.importorskip("torch")
+    lib = native.load()
+    view, border, blend = (3, 3, 2003), (0.5, -5.0, -5.0), (1000.0, 1.0, 1.0)
+    got = _blend_on_device(lib, torch, view, view, border, blend)
+    want = O.transform_weights(view, [1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0], (0, 0, 0), view, border, blend)
+    np.testing.assert_array_equal(got, want)
+    row = want[1, 1]
+    assert row[0] == 0 and np.all(np.diff(row[:1001]) >= 0)
+
+
 def _weights(rng, shape, zero_frac):
-    # a mix of generic floats and products of blending-table values, with zeros
+    # a mix of generic floats and products of blending-table values, with zeros; 3% tiny
+    # values (2^-40 .. 2^-70) and 1% denormals spread the views' exponents beyond what the
+    # kernel's integer sum covers, so those voxels take its double sum
     lut = O._BLEND_LUT.astype(np.float32)
     a = rng.random(shape).astype(np.float32) ** 2
     b = lut[rng.integers(0, 1001, shape)] * lut[rng.integers(0, 1001, shape)]
-    return np.where(rng.random(shape) < zero_frac, 0, np.where(rng.random(shape) < 0.5, a, b)).astype(np.float32)
+    tiny = np.ldexp(rng.random(shape), -rng.integers(40, 71, shape)).astype(np.float32)
+    den = (rng.integers(1, 1 << 23, shape).astype(np.uint32)).view(np.float32)
+    u = rng.random(shape)
+    w = np.where(u < 0.5, a, b)
+    w = np.where(u > 0.97, tiny, np.where(u > 0.96, den, w))
+    return np.where(rng.random(shape) < zero_frac, 0, w).astype(np.float32)
 
 
 @pytest.mark.parametrize("mode", [0, 1])
