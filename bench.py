@@ -54,6 +54,8 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-autotune", action="store_true", help="planner's default tiles instead of timed ones")
+    ap.add_argument("--only", choices=["inputs", "separable"],
+                    help="measure only the input preparation or the separable convolution at the workload's size")
     return ap.parse_args()
 
 
@@ -197,6 +199,10 @@ def run_ours(args, rank, world, local):
     peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
 
     prob = make_problem(args.workload)
+    if args.only:
+        part = {"inputs": ("input_preparation", run_inputs), "separable": ("separable_convolution", run_separable)}
+        key, fn = part[args.only]
+        return {"workload": args.workload, key: fn(prob, local, hbm_peak)}
     n_vox = prob.n_voxels
     V = len(prob.views)
     lib = native.load()

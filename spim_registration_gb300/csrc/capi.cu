@@ -123,14 +123,44 @@ struct PhaseTrace {
     on = e && *e == '1';
     t0 = std::chrono::steady_clock::now();
   }
+  // the phase's wall time, and the part of it the host spent before waiting for the stream
   void mark(const char* what) {
     if (!on) return;
+    auto th = std::chrono::steady_clock::now();
     cudaStreamSynchronize(s);
     auto t1 = std::chrono::steady_clock::now();
-    std::fprintf(stderr, "[mvd_create] %-28s %8.2f ms\n", what,
-                 std::chrono::duration<double, std::milli>(t1 - t0).count());
+    std::fprintf(stderr, "[mvd_create] %-28s %8.2f ms (host %.2f ms)\n", what,
+                 std::chrono::duration<double, std::milli>(t1 - t0).count(),
+                 std::chrono::duration<double, std::milli>(th - t0).count());
     t0 = t1;
   }
+};
+
+// A second stream for the input copies, ordered after the work enqueued so far on `main`;
+// join() makes `main` wait for the copies.  The stream and its events live for one mvd_create.
+struct UploadStream {
+  cudaStream_t main, s = nullptr;
+  cudaEvent_t ready = nullptr, done = nullptr;
+  explicit UploadStream(cudaStream_t m) : main(m) {
+    MVD_CHECK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    MVD_CHECK(cudaEventCreateWithFlags(&ready, cudaEventDisableTiming));
+    MVD_CHECK(cudaEventCreateWithFlags(&done, cudaEventDisableTiming));
+    MVD_CHECK(cudaEventRecord(ready, main));
+    MVD_CHECK(cudaStreamWaitEvent(s, ready, 0));
+  }
+  void join() {
+    MVD_CHECK(cudaEventRecord(done, s));
+    MVD_CHECK(cudaStreamWaitEvent(main, done, 0));
+  }
+  ~UploadStream() {
+    // on an error path the copies may still run: wait for them before the stream goes
+    if (s) cudaStreamSynchronize(s);
+    if (done) cudaEventDestroy(done);
+    if (ready) cudaEventDestroy(ready);
+    if (s) cudaStreamDestroy(s);
+  }
+  UploadStream(const UploadStream&) = delete;
+  UploadStream& operator=(const UploadStream&) = delete;
 };
 
 std::mutex g_ctx_mu;
@@ -632,6 +662,15 @@ std::unique_ptr<ConvPlan> block_plan(PlanTable& pt, const std::array<int, 3>& b,
   return make_conv_plan(pt, b[0], b[1], b[2], k[0], k[1], k[2]);
 }
 
+// view v's kernel spectra (PSF and compound kernel) on its plan's padded tile grid
+void build_view_otfs(mvd_decon* h, int v) {
+  const ConvPlan& p = *h->plans[v];
+  h->otf1[v].alloc(p.otf_elems * sizeof(float2));
+  h->otf2[v].alloc(p.otf_elems * sizeof(float2));
+  build_otf(h->pt, p, h->k1[v].as<float>(), h->otf1[v].as<float2>(), h->scratch, h->stream);
+  build_otf(h->pt, p, h->k2[v].as<float>(), h->otf2[v].as<float2>(), h->scratch, h->stream);
+}
+
 }  // namespace
 
 extern "C" int mvd_create(mvd_decon** out, int devCUDA, const int* dims, int num_views, const float* const* views,
@@ -676,23 +715,30 @@ extern "C" int mvd_create(mvd_decon** out, int devCUDA, const int* dims, int num
   h->k2.resize(num_views);
   h->otf1.resize(num_views);
   h->otf2.resize(num_views);
+  PhaseTrace trace(h->stream);
   for (int v = 0; v < num_views; ++v) {
     h->kd.push_back({psf_dims[3 * v], psf_dims[3 * v + 1], psf_dims[3 * v + 2]});
     h->img[v].alloc(nb);
     h->w[v].alloc(nb);
-    // cudaMemcpyDefault: the inputs may be host memory or device memory (for example views
-    // resampled on the GPU by mvd_transform_view); unified addressing tells them apart
-    MVD_CHECK(cudaMemcpyAsync(h->img[v].p, views[v], nb, cudaMemcpyDefault, h->stream));
-    MVD_CHECK(cudaMemcpyAsync(h->w[v].p, weights[v], nb, cudaMemcpyDefault, h->stream));
     const size_t kb = vox(h->kd[v]) * sizeof(float);
     h->k1[v].alloc(kb);
+    // cudaMemcpyDefault: the inputs may be host memory or device memory (for example views
+    // resampled on the GPU by mvd_transform_view); unified addressing tells them apart
     MVD_CHECK(cudaMemcpyAsync(h->k1[v].p, psfs[v], kb, cudaMemcpyDefault, h->stream));
   }
-  PhaseTrace trace(h->stream);
-  MVD_CHECK(cudaStreamSynchronize(h->stream));
-  trace.mark("upload views/weights/psfs");
+  // The compound kernels need only the PSFs: they are enqueued first, and the views and
+  // weights are copied on a second stream meanwhile (a copy from pageable memory holds the
+  // host until it is done, while the kernels already run).  The buffers were allocated in the
+  // handle stream's order, so the copy stream waits for that point, and the handle stream
+  // waits for the copies before its first use of the data.
+  UploadStream up(h->stream);
   prepare_kernels(h.get());
-  trace.mark("kernel preparation");
+  for (int v = 0; v < num_views; ++v) {
+    MVD_CHECK(cudaMemcpyAsync(h->img[v].p, views[v], nb, cudaMemcpyDefault, up.s));
+    MVD_CHECK(cudaMemcpyAsync(h->w[v].p, weights[v], nb, cudaMemcpyDefault, up.s));
+  }
+  up.join();
+  trace.mark("upload with kernel preparation");
   h->psi.alloc(nb);
   h->q.alloc(nb);
   MVD_CHECK(cudaMemsetAsync(h->psi.p, 0, nb, h->stream));
@@ -734,20 +780,16 @@ extern "C" int mvd_create(mvd_decon** out, int devCUDA, const int* dims, int num
         hi[d] = empty ? dims[d] : b[3 + d] + 1;
       }
       h->plans.push_back(plan_view(h.get(), v, lo, hi, (flags & MVD_FLAG_AUTOTUNE) != 0));
+      // the view's kernel spectra run on the GPU while the host plans the next view
+      build_view_otfs(h.get(), v);
     }
   }
-  trace.mark("data boxes and tile plans");
-  for (int v = 0; v < num_views; ++v) {
-    const ConvPlan& p = *h->plans[v];
-    spec_max = std::max(spec_max, p.spec_elems);
-    h->otf1[v].alloc(p.otf_elems * sizeof(float2));
-    h->otf2[v].alloc(p.otf_elems * sizeof(float2));
-    build_otf(h->pt, p, h->k1[v].as<float>(), h->otf1[v].as<float2>(), h->scratch, h->stream);
-    build_otf(h->pt, p, h->k2[v].as<float>(), h->otf2[v].as<float2>(), h->scratch, h->stream);
-  }
+  if (flags & MVD_FLAG_PLAIN)
+    for (int v = 0; v < num_views; ++v) build_view_otfs(h.get(), v);
+  for (int v = 0; v < num_views; ++v) spec_max = std::max(spec_max, h->plans[v]->spec_elems);
   h->spec.alloc(spec_max * sizeof(float2));
   h->scratch.alloc(0);
-  trace.mark("kernel spectra (OTFs)");
+  trace.mark("tile plans and kernel spectra");
   // first iteration: psi := average intensity of the overlapping area
   h->d_sc.alloc(2 * sizeof(double));
   MVD_CHECK(cudaMemsetAsync(h->d_sc.p, 0, 2 * sizeof(double), h->stream));

@@ -654,18 +654,57 @@ struct ViewPtrs {
 
 // FirstIteration.call (FirstIteration.java:84-154): per voxel the mean of the positive view
 // values; summed (FP64) over voxels with at least one positive value, and counted.
+// hi + lo = a + b exactly (Knuth's two-sum)
+__device__ __forceinline__ void two_sum(float a, float b, float& hi, float& lo) {
+  hi = __fadd_rn(a, b);
+  const float bb = __fsub_rn(hi, a);
+  lo = __fadd_rn(__fsub_rn(a, __fsub_rn(hi, bb)), __fsub_rn(b, bb));
+}
+
+// (hi, lo) += (bh, bl), renormalised; ~2^-44 relative
+__device__ __forceinline__ void pair_add(float& hi, float& lo, float bh, float bl) {
+  float s, e;
+  two_sum(hi, bh, s, e);
+  e = __fadd_rn(e, __fadd_rn(lo, bl));
+  hi = __fadd_rn(s, e);
+  lo = __fsub_rn(e, __fsub_rn(hi, s));
+}
+
+// FirstIteration.compatibleLoop (FirstIteration.java:124-154): per voxel the mean of the
+// views' positive values, summed over the voxels that have any (RealSum), and their count.
+// GB300's FP64 pipe cannot take a double division and six double additions per voxel at
+// HBM speed, so each thread carries its sum as a float pair (the voxel's view sum by exact
+// two-sums, times 1/c as a pair), flushed into a double every 16 voxels.  The reference's
+// RealSum is itself order-dependent; each pair chunk is accurate to ~2^-43.
 __global__ void first_iteration_kernel(ViewPtrs v, int nviews, long long n, double* out) {
-  double sum = 0.0, cnt = 0.0;
+  float acc_hi = 0.f, acc_lo = 0.f;
+  double total = 0.0;
+  unsigned long long cnt = 0;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-    double s = 0.0;
+    float s_hi = 0.f, s_lo = 0.f;
     int c = 0;
     for (int k = 0; k < nviews; ++k) {
       const float x = __ldg(v.p[k] + i);
-      if (x > 0.f) { s += (double)x; ++c; }
+      if (x > 0.f) {
+        float e;
+        two_sum(s_hi, x, s_hi, e);
+        s_lo = __fadd_rn(s_lo, e);
+        ++c;
+      }
     }
-    if (c > 0) { sum += s / c; cnt += 1.0; }
+    if (c > 0) {
+      // (s_hi + s_lo) / c: q = s_hi / c rounded, the remainder s_hi - q c is exact (an FMA)
+      const float fc = (float)c;
+      const float q = __fdiv_rn(s_hi, fc);
+      const float r = __fadd_rn(__fmaf_rn(-q, fc, s_hi), s_lo);
+      pair_add(acc_hi, acc_lo, q, __fdiv_rn(r, fc));
+      if ((++cnt & 15) == 0) {
+        total += (double)acc_hi + (double)acc_lo;
+        acc_hi = acc_lo = 0.f;
+      }
+    }
   }
-  block_reduce_add2(sum, cnt, out);
+  block_reduce_add2(total + ((double)acc_hi + (double)acc_lo), (double)cnt, out);
 }
 
 void dev_first_iteration(const float* const* views, int nviews, long long n, double* out, cudaStream_t s) {

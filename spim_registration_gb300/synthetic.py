@@ -158,7 +158,10 @@ _BLEND_LUT = np.array(
 
 
 def blending_weight(q_xyz: np.ndarray, dims_xyz, border_xyz, range_xyz) -> np.ndarray:
-    """Cosine blending weight at real positions (BlendingRealRandomAccess.computeWeight :91-121)."""
+    """Cosine blending weight at real positions (BlendingRealRandomAccess.computeWeight :91-121),
+    for generating test volumes only: the table holds exact k/1000 values and the index rounds
+    half to even, where the reference accumulates d and rounds half up (the GPU input
+    preparation follows the reference bit for bit)."""
     w = np.ones(q_xyz.shape[:-1], dtype=np.float32)
     zero = np.zeros(q_xyz.shape[:-1], dtype=bool)
     for d in range(3):
