@@ -136,32 +136,58 @@ struct PhaseTrace {
   }
 };
 
-// A second stream for the input copies, ordered after the work enqueued so far on `main`;
-// join() makes `main` wait for the copies.  The stream and its events live for one mvd_create.
-struct UploadStream {
-  cudaStream_t main, s = nullptr;
-  cudaEvent_t ready = nullptr, done = nullptr;
-  explicit UploadStream(cudaStream_t m) : main(m) {
-    MVD_CHECK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+// n side streams forked from `main`: each starts after the work enqueued so far on `main`,
+// and join() makes `main` wait for all of them.  Streams and events are released when the
+// object goes (CUDA frees them once their work is done); if join() was never reached (an
+// error path), the side streams are waited for first, since buffers they use may be freed.
+struct ForkedStreams {
+  cudaStream_t main;
+  std::vector<cudaStream_t> s;
+  std::vector<cudaEvent_t> done;
+  cudaEvent_t ready = nullptr;
+  bool joined = false;
+  ForkedStreams(cudaStream_t m, int n) : main(m) {
     MVD_CHECK(cudaEventCreateWithFlags(&ready, cudaEventDisableTiming));
-    MVD_CHECK(cudaEventCreateWithFlags(&done, cudaEventDisableTiming));
     MVD_CHECK(cudaEventRecord(ready, main));
-    MVD_CHECK(cudaStreamWaitEvent(s, ready, 0));
+    for (int i = 0; i < n; ++i) {
+      cudaStream_t st;
+      MVD_CHECK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+      s.push_back(st);
+      cudaEvent_t e;
+      MVD_CHECK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+      done.push_back(e);
+      MVD_CHECK(cudaStreamWaitEvent(st, ready, 0));
+    }
   }
   void join() {
-    MVD_CHECK(cudaEventRecord(done, s));
-    MVD_CHECK(cudaStreamWaitEvent(main, done, 0));
+    for (size_t i = 0; i < s.size(); ++i) {
+      MVD_CHECK(cudaEventRecord(done[i], s[i]));
+      MVD_CHECK(cudaStreamWaitEvent(main, done[i], 0));
+    }
+    joined = true;
   }
-  ~UploadStream() {
-    // on an error path the copies may still run: wait for them before the stream goes
-    if (s) cudaStreamSynchronize(s);
-    if (done) cudaEventDestroy(done);
+  ~ForkedStreams() {
+    for (size_t i = 0; i < s.size(); ++i) {
+      if (!joined) cudaStreamSynchronize(s[i]);
+      cudaEventDestroy(done[i]);
+      cudaStreamDestroy(s[i]);
+    }
     if (ready) cudaEventDestroy(ready);
-    if (s) cudaStreamDestroy(s);
   }
-  UploadStream(const UploadStream&) = delete;
-  UploadStream& operator=(const UploadStream&) = delete;
+  ForkedStreams(const ForkedStreams&) = delete;
+  ForkedStreams& operator=(const ForkedStreams&) = delete;
 };
+
+// whether copying from p returns before the copy is done (device memory, or host memory
+// that is page-locked); a copy from pageable host memory holds the calling thread
+bool async_copy_source(const void* p) {
+  cudaPointerAttributes a{};
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged || a.type == cudaMemoryTypeHost;
+}
 
 std::mutex g_ctx_mu;
 std::unordered_map<int, std::unique_ptr<DeviceCtx>> g_ctx;
@@ -523,69 +549,113 @@ void prepare_kernels(mvd_decon* h) {
   cudaStream_t s = h->stream;
   long long kmax = 0;
   for (int v = 0; v < V; ++v) kmax = std::max(kmax, vox(h->kd[v]));
-  DevBuf A(kmax * sizeof(float)), B(kmax * sizeof(float)), C(kmax * sizeof(float)), sum(sizeof(double));
-  DevBuf otf, spec;
-  std::map<std::vector<int>, std::unique_ptr<ConvPlan>> plans;
-  auto norm = [&](float* k, long long n) {
-    MVD_CHECK(cudaMemsetAsync(sum.p, 0, sizeof(double), s));
-    dev_sum_f64(k, n, sum.as<double>(), s);
-    dev_scale_div(k, n, sum.as<double>(), s);
-  };
-  auto mirror = [&](const float* in, const std::array<int, 3>& d, float* out) {
-    dev_mirror(in, out, d[0], d[1], d[2], s);
-  };
-  // out = ext0(in) (*) kern over in's dims
-  auto conv0 = [&](const float* in, const std::array<int, 3>& d, const float* kern, const std::array<int, 3>& kd,
-                   float* out) {
-    const std::vector<int> key{d[0], d[1], d[2], kd[0], kd[1], kd[2]};
-    auto& plan = plans[key];
-    if (!plan) plan = make_conv_plan(h->pt, d[0], d[1], d[2], kd[0], kd[1], kd[2]);
-    otf.ensure(plan->otf_elems * sizeof(float2));
-    spec.ensure(plan->spec_elems * sizeof(float2));
-    build_otf(h->pt, *plan, kern, otf.as<float2>(), h->scratch, s);
-    convolve(h->pt, *plan, in, Ext::Value, 0.f, otf.as<float2>(), spec.as<float2>(), out, s);
-  };
-  for (int v = 0; v < V; ++v) norm(h->k1[v].as<float>(), vox(h->kd[v]));
-  for (int v = 0; v < V; ++v) {
-    const auto& dv = h->kd[v];
-    const long long nv = vox(dv);
-    h->k2[v].alloc(nv * sizeof(float));
-    float* k2 = h->k2[v].as<float>();
-    const float* k1 = h->k1[v].as<float>();
-    if (V == 1 || h->psftype == MVD_INDEPENDENT) {
-      mirror(k1, dv, k2);
-    } else if (h->psftype == MVD_EFFICIENT_BAYESIAN) {
-      // P_v^compound = P_v* prod_{w != v} crop(crop(P_v* (*) P_w) (*) P_w*)
-      mirror(k1, dv, k2);
-      for (int wv = 0; wv < V; ++wv) {
-        if (wv == v) continue;
-        mirror(k1, dv, A.as<float>());
-        conv0(A.as<float>(), dv, h->k1[wv].as<float>(), h->kd[wv], B.as<float>());
-        mirror(h->k1[wv].as<float>(), h->kd[wv], C.as<float>());
-        conv0(B.as<float>(), dv, C.as<float>(), h->kd[wv], A.as<float>());
-        dev_mul(k2, A.as<float>(), nv, s);
-      }
-      norm(k2, nv);
-    } else if (h->psftype == MVD_OPTIMIZATION_I) {
-      // mirror(norm(P_v prod_{w != v} crop(P_v (*) P_w*)))
-      MVD_CHECK(cudaMemcpyAsync(A.p, k1, nv * sizeof(float), cudaMemcpyDeviceToDevice, s));
-      for (int wv = 0; wv < V; ++wv) {
-        if (wv == v) continue;
-        mirror(h->k1[wv].as<float>(), h->kd[wv], C.as<float>());
-        conv0(k1, dv, C.as<float>(), h->kd[wv], B.as<float>());
-        dev_mul(A.as<float>(), B.as<float>(), nv, s);
-      }
-      norm(A.as<float>(), nv);
-      mirror(A.as<float>(), dv, k2);
-    } else {
-      // OPTIMIZATION_II: mirror(norm(P_v ^ V))
-      MVD_CHECK(cudaMemcpyAsync(A.p, k1, nv * sizeof(float), cudaMemcpyDeviceToDevice, s));
-      dev_pow(A.as<float>(), V, nv, s);
-      norm(A.as<float>(), nv);
-      mirror(A.as<float>(), dv, k2);
+  // every view's compound kernel reads all normalised PSFs: normalise them first
+  {
+    DevBuf sum(sizeof(double));
+    for (int v = 0; v < V; ++v) {
+      MVD_CHECK(cudaMemsetAsync(sum.p, 0, sizeof(double), s));
+      dev_sum_f64(h->k1[v].as<float>(), vox(h->kd[v]), sum.as<double>(), s);
+      dev_scale_div(h->k1[v].as<float>(), vox(h->kd[v]), sum.as<double>(), s);
     }
   }
-  // the scratch buffers and plans go out of scope: freed in the stream's order
+  // The plans of the PSF-pair convolutions (view v's PSF volume with view w's PSF) are built
+  // here, with their tables uploaded in the handle stream's order, and each view gets scratch
+  // sized for all of them, so that nothing is allocated while the views' chains run.
+  const bool pairs = V > 1 && (h->psftype == MVD_EFFICIENT_BAYESIAN || h->psftype == MVD_OPTIMIZATION_I);
+  std::map<std::vector<int>, std::unique_ptr<ConvPlan>> plans;
+  size_t otf_max = 1, spec_max = 1, real_max = 1;
+  auto plan_for = [&](const std::array<int, 3>& d, const std::array<int, 3>& kd) -> ConvPlan& {
+    const std::vector<int> key{d[0], d[1], d[2], kd[0], kd[1], kd[2]};
+    auto& plan = plans[key];
+    if (!plan) {
+      plan = make_conv_plan(h->pt, d[0], d[1], d[2], kd[0], kd[1], kd[2]);
+      otf_max = std::max<size_t>(otf_max, plan->otf_elems);
+      spec_max = std::max<size_t>(spec_max, plan->spec_elems);
+      real_max = std::max<size_t>(real_max, (size_t)plan->ax.T * plan->ay.T * plan->az.T);
+    }
+    return *plan;
+  };
+  if (pairs)
+    for (int v = 0; v < V; ++v)
+      for (int wv = 0; wv < V; ++wv)
+        if (wv != v) plan_for(h->kd[v], h->kd[wv]);
+  h->pt.device();  // upload the FFT table with every length the plans added
+  struct Scratch {
+    DevBuf A, B, C, sum, otf, spec, real;
+  };
+  std::vector<Scratch> sc(V);
+  for (int v = 0; v < V; ++v) {
+    h->k2[v].alloc(vox(h->kd[v]) * sizeof(float));
+    Scratch& x = sc[v];
+    x.A.alloc(kmax * sizeof(float));
+    x.B.alloc(kmax * sizeof(float));
+    x.C.alloc(kmax * sizeof(float));
+    x.sum.alloc(sizeof(double));
+    if (pairs) {
+      x.otf.alloc(otf_max * sizeof(float2));
+      x.spec.alloc(spec_max * sizeof(float2));
+      x.real.alloc(real_max * sizeof(float));
+    }
+  }
+  // Each view's chain of small launches runs on its own stream: the chains are independent
+  // and their kernels are far too small to fill the GPU one at a time.
+  ForkedStreams fork(s, V);
+  for (int v = 0; v < V; ++v) {
+    cudaStream_t st = fork.s[v];
+    Scratch& x = sc[v];
+    const auto& dv = h->kd[v];
+    const long long nv = vox(dv);
+    float* k2 = h->k2[v].as<float>();
+    const float* k1 = h->k1[v].as<float>();
+    auto norm = [&](float* k) {
+      MVD_CHECK(cudaMemsetAsync(x.sum.p, 0, sizeof(double), st));
+      dev_sum_f64(k, nv, x.sum.as<double>(), st);
+      dev_scale_div(k, nv, x.sum.as<double>(), st);
+    };
+    // out = ext0(in) (*) kern over in's dims
+    auto conv0 = [&](const float* in, const float* kern, const std::array<int, 3>& kd, float* out) {
+      ConvPlan& plan = plan_for(dv, kd);
+      build_otf(h->pt, plan, kern, x.otf.as<float2>(), x.real, st);
+      convolve(h->pt, plan, in, Ext::Value, 0.f, x.otf.as<float2>(), x.spec.as<float2>(), out, st);
+    };
+    if (V == 1 || h->psftype == MVD_INDEPENDENT) {
+      dev_mirror(k1, k2, dv[0], dv[1], dv[2], st);
+    } else if (h->psftype == MVD_EFFICIENT_BAYESIAN) {
+      // P_v^compound = P_v* prod_{w != v} crop(crop(P_v* (*) P_w) (*) P_w*)
+      dev_mirror(k1, k2, dv[0], dv[1], dv[2], st);
+      for (int wv = 0; wv < V; ++wv) {
+        if (wv == v) continue;
+        const auto& dw = h->kd[wv];
+        dev_mirror(k1, x.A.as<float>(), dv[0], dv[1], dv[2], st);
+        conv0(x.A.as<float>(), h->k1[wv].as<float>(), dw, x.B.as<float>());
+        dev_mirror(h->k1[wv].as<float>(), x.C.as<float>(), dw[0], dw[1], dw[2], st);
+        conv0(x.B.as<float>(), x.C.as<float>(), dw, x.A.as<float>());
+        dev_mul(k2, x.A.as<float>(), nv, st);
+      }
+      norm(k2);
+    } else if (h->psftype == MVD_OPTIMIZATION_I) {
+      // mirror(norm(P_v prod_{w != v} crop(P_v (*) P_w*)))
+      MVD_CHECK(cudaMemcpyAsync(x.A.p, k1, nv * sizeof(float), cudaMemcpyDeviceToDevice, st));
+      for (int wv = 0; wv < V; ++wv) {
+        if (wv == v) continue;
+        const auto& dw = h->kd[wv];
+        dev_mirror(h->k1[wv].as<float>(), x.C.as<float>(), dw[0], dw[1], dw[2], st);
+        conv0(k1, x.C.as<float>(), dw, x.B.as<float>());
+        dev_mul(x.A.as<float>(), x.B.as<float>(), nv, st);
+      }
+      norm(x.A.as<float>());
+      dev_mirror(x.A.as<float>(), k2, dv[0], dv[1], dv[2], st);
+    } else {
+      // OPTIMIZATION_II: mirror(norm(P_v ^ V))
+      MVD_CHECK(cudaMemcpyAsync(x.A.p, k1, nv * sizeof(float), cudaMemcpyDeviceToDevice, st));
+      dev_pow(x.A.as<float>(), V, nv, st);
+      norm(x.A.as<float>());
+      dev_mirror(x.A.as<float>(), k2, dv[0], dv[1], dv[2], st);
+    }
+  }
+  fork.join();
+  // the scratch buffers and plans go out of scope after the join: freed in the handle
+  // stream's order, behind the views' chains
 }
 
 // A view's convolutions only need to cover the bounding box of its data or weight (img > 0
@@ -726,17 +796,25 @@ extern "C" int mvd_create(mvd_decon** out, int devCUDA, const int* dims, int num
     // resampled on the GPU by mvd_transform_view); unified addressing tells them apart
     MVD_CHECK(cudaMemcpyAsync(h->k1[v].p, psfs[v], kb, cudaMemcpyDefault, h->stream));
   }
-  // The compound kernels need only the PSFs: they are enqueued first, and the views and
-  // weights are copied on a second stream meanwhile (a copy from pageable memory holds the
-  // host until it is done, while the kernels already run).  The buffers were allocated in the
-  // handle stream's order, so the copy stream waits for that point, and the handle stream
-  // waits for the copies before its first use of the data.
-  UploadStream up(h->stream);
+  // The compound kernels need only the PSFs, so they run while the views and weights are
+  // copied on a side stream.  The buffers were allocated in the handle stream's order, so the
+  // copy stream starts after that point, and the handle stream waits for the copies before its
+  // first use of the data.  Copies from device or page-locked memory return at once and are
+  // enqueued first; a copy from pageable memory holds the host until it is done, so the
+  // kernels are enqueued before those.
+  bool async_src = true;
+  for (int v = 0; v < num_views; ++v)
+    async_src = async_src && async_copy_source(views[v]) && async_copy_source(weights[v]);
+  ForkedStreams up(h->stream, 1);
+  auto copy_inputs = [&] {
+    for (int v = 0; v < num_views; ++v) {
+      MVD_CHECK(cudaMemcpyAsync(h->img[v].p, views[v], nb, cudaMemcpyDefault, up.s[0]));
+      MVD_CHECK(cudaMemcpyAsync(h->w[v].p, weights[v], nb, cudaMemcpyDefault, up.s[0]));
+    }
+  };
+  if (async_src) copy_inputs();
   prepare_kernels(h.get());
-  for (int v = 0; v < num_views; ++v) {
-    MVD_CHECK(cudaMemcpyAsync(h->img[v].p, views[v], nb, cudaMemcpyDefault, up.s));
-    MVD_CHECK(cudaMemcpyAsync(h->w[v].p, weights[v], nb, cudaMemcpyDefault, up.s));
-  }
+  if (!async_src) copy_inputs();
   up.join();
   trace.mark("upload with kernel preparation");
   h->psi.alloc(nb);

@@ -319,6 +319,7 @@ bool volume_box_map(const float* base, int nx, int ny, int nz, int w, int h, CUt
           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
     return false;
+  if (cache.size() >= 4096) cache.clear();  // maps are cheap to encode again; bound the memory
   cache[key] = m;
   *out = m;
   return true;
