@@ -4,6 +4,8 @@ The reference ships no tests or golden vectors for this path, so the oracle is p
 mathematical identities of the restated algorithm and by the committed golden fixtures that
 tests/golden/make_golden.py generates from it.
 """
+import math
+
 import numpy as np
 import pytest
 
@@ -195,6 +197,18 @@ def test_transform_input_identity_and_shift():
     out = O.transform_input(view, shifted, (0, 0, 0), (6, 7, 10))
     np.testing.assert_allclose(out[:, :, 2:], view, rtol=1e-12)
     assert np.all(out[:, :, :2] == 0)
+
+
+def test_blend_table_follows_the_reference_fill_loop():
+    """BlendingRealRandomAccess fills its table by stepping d += 0.001 in double
+    (BlendingRealRandomAccess.java:47-53): entry k holds the value at the accumulated d, whose
+    last bits drift from k / 1000 (most doubles differ, no float does)."""
+    lut = O._BLEND_LUT
+    assert lut.shape == (1001,) and lut[0] == 0.0 and lut[1000] == 1.0
+    exact = np.array([(math.cos((1 - k / 1000.0) * math.pi) + 1) / 2 for k in range(1001)])
+    assert (lut != exact).sum() > 800
+    np.testing.assert_array_equal(lut.astype(np.float32), exact.astype(np.float32))
+    assert np.all(np.diff(lut) >= 0)
 
 
 def test_blending_weights_profile():
