@@ -66,17 +66,18 @@ __device__ __forceinline__ float trilinear_mirror(const float* __restrict__ img,
   return acc;
 }
 
-// The reference normalises in double; GB300's FP64 pipe is a small fraction of its FP32 one.
-// The sum over the views stays in double (the reference's sequential double sum cannot be
-// reproduced otherwise), but the per-view quotients and OSEM products are carried as
-// unevaluated float pairs (hi + lo, within ~2^-44 relative of the exact value) built from
-// error-free transformations, rounded once at the end.  Each rounding is certified: when the
-// pair lies within 2^-14 of a half ulp from a rounding boundary (or the result is a power of
-// two or denormal), only the reference's double rounding decides it.  Such voxels are left
-// unwritten and appended to a list (warp-aggregated atomics), which a second kernel finishes
-// with the reference's double arithmetic, so no warp diverges into the double path.  They are
-// rare for a generic OSEM factor (~1e-4) but common for decimal ones: w * 1.7 is an exact tie
-// in rational arithmetic for ~5% of floats w, and the double 1.7 sits just beside it.
+// The reference normalises in double (and multiplies blending weights by a double table);
+// GB300's FP64 pipe is a small fraction of its FP32 one.  The sum over the views is
+// reproduced exactly in 64-bit integers (exact_view_sum below); the per-view quotients and
+// OSEM products, and the blending products, are carried as unevaluated float pairs (hi + lo,
+// within ~2^-44 relative of the exact value) built from error-free transformations, rounded
+// once at the end.  Each rounding is certified: when the pair lies within 2^-14 of a half ulp
+// from a rounding boundary (or the result is tiny or an inexact power of two), only the
+// reference's double rounding decides it.  The normalisation leaves such voxels unwritten and
+// appends them to a list (warp-aggregated atomics), which a second kernel finishes with the
+// reference's double arithmetic, so no warp diverges into the double path.  They are rare for
+// a generic OSEM factor (~1e-4) but common for decimal ones: w * 1.7 is an exact tie in
+// rational arithmetic for ~5% of floats w, and the double 1.7 sits just beside it.
 
 struct FF {  // hi + lo
   float hi, lo;
@@ -158,8 +159,23 @@ __device__ __forceinline__ float blend_weight(float lx, float ly, float lz, int 
   return w;
 }
 
-// One thread per output voxel; a block covers a 32 x 8 patch of one z plane, so its view
-// positions stay close together whatever the rotation (the view's reads hit L1/L2).
+// Output voxel (x, y, z): the resampled view (0 outside it) and its blending weight.
+template <class Index>
+__device__ __forceinline__ void transform_voxel(const float* __restrict__ view, int sx, int sy, int sz,
+                                                const Affine& inv, float s0, float s1, float s2, bool want_img,
+                                                bool want_blend, float3 border, float3 range, float& v, float& wgt) {
+  const float t0 = inv.m[0] * s0 + inv.m[1] * s1 + inv.m[2] * s2 + inv.m[3];
+  const float t1 = inv.m[4] * s0 + inv.m[5] * s1 + inv.m[6] * s2 + inv.m[7];
+  const float t2 = inv.m[8] * s0 + inv.m[9] * s1 + inv.m[10] * s2 + inv.m[11];
+  v = 0.f;  // no image data (MVDeconvolution.computeQuotient reads 0 as "no data")
+  if (want_img && t0 >= 0.f && t1 >= 0.f && t2 >= 0.f && t0 < (float)sx && t1 < (float)sy && t2 < (float)sz)
+    v = fmaxf(1e-4f, trilinear_mirror<Index>(view, sx, sy, sz, t0, t1, t2));
+  // the blending weight is defined everywhere (the border can be negative)
+  wgt = want_blend ? blend_weight(t0, t1, t2, sx, sy, sz, border, range) : 0.f;
+}
+
+// One thread per output voxel; a block covers a 32 x 8 patch of one z plane, so a warp runs
+// along output x.  For views whose x axis lies closer to output x than to output z.
 template <class Index>
 __global__ void __launch_bounds__(256) transform_view_kernel(const float* __restrict__ view, int sx, int sy, int sz,
                                                              Affine inv, int ox, int oy, int oz, int nx, int ny,
@@ -169,18 +185,48 @@ __global__ void __launch_bounds__(256) transform_view_kernel(const float* __rest
   const int x = blockIdx.x * 32 + threadIdx.x, y = blockIdx.y * 8 + threadIdx.y, z = blockIdx.z;
   if (x >= nx || y >= ny) return;
   const long long i = ((long long)z * ny + y) * nx + x;
-  const float s0 = (float)(x + ox), s1 = (float)(y + oy), s2 = (float)(z + oz);
-  const float t0 = inv.m[0] * s0 + inv.m[1] * s1 + inv.m[2] * s2 + inv.m[3];
-  const float t1 = inv.m[4] * s0 + inv.m[5] * s1 + inv.m[6] * s2 + inv.m[7];
-  const float t2 = inv.m[8] * s0 + inv.m[9] * s1 + inv.m[10] * s2 + inv.m[11];
-  if (out_img) {
-    float v = 0.f;  // no image data (MVDeconvolution.computeQuotient reads 0 as "no data")
-    if (t0 >= 0.f && t1 >= 0.f && t2 >= 0.f && t0 < (float)sx && t1 < (float)sy && t2 < (float)sz)
-      v = fmaxf(1e-4f, trilinear_mirror<Index>(view, sx, sy, sz, t0, t1, t2));
-    out_img[i] = v;
+  float v, wgt;
+  transform_voxel<Index>(view, sx, sy, sz, inv, (float)(x + ox), (float)(y + oy), (float)(z + oz), out_img != nullptr,
+                         out_blend != nullptr, border, range, v, wgt);
+  if (out_img) out_img[i] = v;
+  if (out_blend) out_blend[i] = wgt;
+}
+
+// The same for views whose x axis lies closer to output z (a rotation near 90 degrees about
+// y): a block covers 32 z x 32 x of one y row and a warp runs along output z, so its lanes
+// read neighbouring voxels of one view row instead of 32 view planes.  The results are staged
+// in shared memory (rows padded to 33: conflict-free both ways) and stored along x.
+template <class Index>
+__global__ void __launch_bounds__(256) transform_view_zfast_kernel(
+    const float* __restrict__ view, int sx, int sy, int sz, Affine inv, int ox, int oy, int oz, int nx, int ny,
+    int nz, float* __restrict__ out_img, float* __restrict__ out_blend, float3 border, float3 range) {
+  __shared__ float s_img[32][33], s_w[32][33];  // [z][x] within the tile
+  const int lane = threadIdx.x, warp = threadIdx.y;
+  const int x0 = blockIdx.x * 32, y = blockIdx.y, z0 = blockIdx.z * 32;
+  const int z = z0 + lane;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const int xl = warp + 8 * k, x = x0 + xl;
+    if (x < nx && z < nz) {
+      float v, wgt;
+      transform_voxel<Index>(view, sx, sy, sz, inv, (float)(x + ox), (float)(y + oy), (float)(z + oz),
+                             out_img != nullptr, out_blend != nullptr, border, range, v, wgt);
+      s_img[lane][xl] = v;
+      s_w[lane][xl] = wgt;
+    }
   }
-  // the blending weight is defined everywhere (the border can be negative)
-  if (out_blend) out_blend[i] = blend_weight(t0, t1, t2, sx, sy, sz, border, range);
+  __syncthreads();
+  const int x = x0 + lane;
+  if (x >= nx) return;
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const int zl = warp + 8 * j, zz = z0 + zl;
+    if (zz < nz) {
+      const long long i = ((long long)zz * ny + y) * nx + x;
+      if (out_img) out_img[i] = s_img[zl][lane];
+      if (out_blend) out_blend[i] = s_w[zl][lane];
+    }
+  }
 }
 
 struct WeightPtrs {
@@ -538,11 +584,21 @@ extern "C" int mvd_transform_view(const float* view, const int* vd, const double
       set_last_error("output height above 524280 or depth above 65535");
       return MVD_ERR_ARG;
     }
-    const dim3 grid((od[0] + 31) / 32, (od[1] + 7) / 8, od[2]);
     const bool narrow = (long long)vd[0] * vd[1] * vd[2] < (1LL << 31);
-    (narrow ? transform_view_kernel<int> : transform_view_kernel<long long>)<<<grid, dim3(32, 8), 0,
-                                                                              static_cast<cudaStream_t>(stream)>>>(
-        view, vd[0], vd[1], vd[2], inv, offset[0], offset[1], offset[2], od[0], od[1], out_img, out_blend, b, r);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    // the warp runs along the output axis that moves the view position most along view x
+    // (inv.m[0] and inv.m[2]: d(view x) / d(output x) and d(view x) / d(output z))
+    if (std::fabs(inv.m[2]) > std::fabs(inv.m[0]) && od[1] <= 65535) {
+      const dim3 grid((od[0] + 31) / 32, od[1], (od[2] + 31) / 32);
+      (narrow ? transform_view_zfast_kernel<int> : transform_view_zfast_kernel<long long>)<<<grid, dim3(32, 8), 0,
+                                                                                              s>>>(
+          view, vd[0], vd[1], vd[2], inv, offset[0], offset[1], offset[2], od[0], od[1], od[2], out_img, out_blend, b,
+          r);
+    } else {
+      const dim3 grid((od[0] + 31) / 32, (od[1] + 7) / 8, od[2]);
+      (narrow ? transform_view_kernel<int> : transform_view_kernel<long long>)<<<grid, dim3(32, 8), 0, s>>>(
+          view, vd[0], vd[1], vd[2], inv, offset[0], offset[1], offset[2], od[0], od[1], out_img, out_blend, b, r);
+    }
     MVD_CHECK(cudaGetLastError());
     count_launch();
     return MVD_OK;
