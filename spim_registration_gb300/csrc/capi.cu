@@ -356,13 +356,17 @@ struct StatSlot {
   unsigned pad;
 };
 
-__global__ void archive_stats_kernel(StatSlot* slot, double* hist, const int* iter, int view, int nviews) {
+// Copies the view's statistics into the history and clears its slot for the view's next
+// update (the slots start cleared); after the last view the iteration counter advances.  This
+// keeps a view's bookkeeping to one small node in the iteration graph.
+__global__ void archive_stats_kernel(StatSlot* slot, double* hist, int* iter, int view, int nviews) {
   const int it = *iter % kHist;
   hist[(it * nviews + view) * 2 + 0] = slot->sum;
   hist[(it * nviews + view) * 2 + 1] = (double)__uint_as_float(slot->max_bits);
+  slot->sum = 0.0;
+  slot->max_bits = 0u;
+  if (view == nviews - 1) *iter += 1;
 }
-
-__global__ void advance_iter_kernel(int* iter) { *iter += 1; }
 
 struct Block {
   int off[3], eoff[3], esz[3], local[3];
@@ -451,7 +455,6 @@ struct mvd_decon {
 
   void enqueue_view(int v) {
     cudaStream_t s = stream;
-    MVD_CHECK(cudaMemsetAsync(slot(v), 0, sizeof(StatSlot), s));
     if (flags & MVD_FLAG_PLAIN) {
       enqueue_view_plain(v);
     } else {
@@ -493,9 +496,6 @@ struct mvd_decon {
 
   void enqueue_iteration() {
     for (int v = 0; v < V; ++v) enqueue_view(v);
-    advance_iter_kernel<<<1, 1, 0, stream>>>(d_iter.as<int>());
-    MVD_CHECK(cudaGetLastError());
-    count_launch();
   }
 
   void run_iteration() {
@@ -907,13 +907,8 @@ extern "C" int mvd_run_view(mvd_decon* h, int view) {
   if (!h) return fail(MVD_ERR_ARG, "NULL handle");
   if (view < 0 || view >= h->V) return fail(MVD_ERR_ARG, "view out of range");
   MVD_CHECK(cudaSetDevice(h->dev));
-  h->enqueue_view(view);
-  if (view == h->V - 1) {
-    advance_iter_kernel<<<1, 1, 0, h->stream>>>(h->d_iter.as<int>());
-    MVD_CHECK(cudaGetLastError());
-    count_launch();
-    ++h->iteration;
-  }
+  h->enqueue_view(view);  // the last view's archive advances the device-side counter
+  if (view == h->V - 1) ++h->iteration;
   return MVD_OK;
   MVD_API_END
 }
@@ -1076,8 +1071,6 @@ extern "C" int mvd_profile_iteration(mvd_decon* h, double* ms, int* launches) {
   for (int v = 0; v < h->V; ++v) {
     const ConvPlan& p = *h->plans[v];
     float2* sp = h->spec.as<float2>();
-    MVD_CHECK(cudaMemsetAsync(h->slot(v), 0, sizeof(StatSlot), s));
-    mark(4);
     launch_fwd_mirror(h->pt, p, h->psi.as<float>(), sp, s);
     mark(0);
     launch_z(h->pt, p, sp, h->otf1[v].as<float2>(), s);
@@ -1095,9 +1088,6 @@ extern "C" int mvd_profile_iteration(mvd_decon* h, double* ms, int* launches) {
     MVD_CHECK(cudaGetLastError());
     mark(4);
   }
-  advance_iter_kernel<<<1, 1, 0, s>>>(h->d_iter.as<int>());
-  MVD_CHECK(cudaGetLastError());
-  mark(4);
   MVD_CHECK(cudaStreamSynchronize(s));
   for (size_t i = 1; i < ev.size(); ++i) {
     float t = 0.f;
@@ -1105,10 +1095,10 @@ extern "C" int mvd_profile_iteration(mvd_decon* h, double* ms, int* launches) {
     ms[kind[i]] += t;
     launches[kind[i]] += 1;
   }
-  launches[4] = h->V + 1;  // archive kernels + the iteration counter
+  launches[4] = h->V;  // the archive kernels (the last one advances the iteration counter)
   for (auto e : ev) cudaEventDestroy(e);
   ++h->iteration;
-  h->launches += 6 * h->V + h->V + 1;
+  h->launches += 6 * h->V + h->V;
   return MVD_OK;
   MVD_API_END
 }
