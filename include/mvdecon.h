@@ -70,6 +70,13 @@ enum {
   MVD_FLAG_AUTOTUNE = 4  /* time candidate tile plans per view at creation and keep the fastest */
 };
 
+/* AdjustInput.sumImg's dependence on the thread count (AdjustInput.java:114-118): the Java code
+ * adds the sum of portion 0 of FusionHelper.divideIntoPortions(n, 2 t) twice, so with t threads
+ * each PSF and compound kernel is divided by its sum plus that portion's sum.  OR-ing
+ * MVD_FLAG_REF_SUM_THREADS(t) (1 <= t <= 32767) into mvd_create's flags reproduces that
+ * normalisation; without it every kernel is divided by its plain FP64 sum (unit sum). */
+#define MVD_FLAG_REF_SUM_THREADS(t) ((int)((unsigned)(t) << 16))
+
 /* Last error message of the calling thread ("" if none). */
 const char* mvd_last_error(void);
 

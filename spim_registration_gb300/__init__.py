@@ -8,6 +8,7 @@ from .mvdecon import (  # noqa: F401
     FLAG_AUTOTUNE,
     FLAG_NO_GRAPH,
     FLAG_PLAIN,
+    FLAG_REF_SUM_THREADS,
     PSFTYPE,
     CUDAFourierConvolution,
     Deconvolution,

@@ -419,6 +419,7 @@ struct mvd_decon {
   int psftype = 0;
   float lambda = 0.f;
   int flags = 0;
+  int ref_sum_threads = 0;  // AdjustInput.sumImg's thread count, 0 = plain sums
   std::vector<std::array<int, 3>> kd;
   DevBuf psi, q, tmp2, spec, scratch;
   std::vector<DevBuf> img, w, k1, k2, otf1, otf2;
@@ -549,14 +550,22 @@ void prepare_kernels(mvd_decon* h) {
   cudaStream_t s = h->stream;
   long long kmax = 0;
   for (int v = 0; v < V; ++v) kmax = std::max(kmax, vox(h->kd[v]));
+  // AdjustInput.normImg: k /= sum(k), where the reference's sum counts portion 0 of
+  // divideIntoPortions(n, 2 t) twice when run with t threads (AdjustInput.java:114-118)
+  const int T = h->ref_sum_threads;
+  auto norm_kernel = [T](float* k, long long n, double* sum, cudaStream_t st) {
+    MVD_CHECK(cudaMemsetAsync(sum, 0, sizeof(double), st));
+    dev_sum_f64(k, n, sum, st);
+    if (T > 0) {
+      const long long first = n / (2LL * T);  // portion 0 = [0, n / (2 t))
+      if (first > 0) dev_sum_f64(k, first, sum, st);
+    }
+    dev_scale_div(k, n, sum, st);
+  };
   // every view's compound kernel reads all normalised PSFs: normalise them first
   {
     DevBuf sum(sizeof(double));
-    for (int v = 0; v < V; ++v) {
-      MVD_CHECK(cudaMemsetAsync(sum.p, 0, sizeof(double), s));
-      dev_sum_f64(h->k1[v].as<float>(), vox(h->kd[v]), sum.as<double>(), s);
-      dev_scale_div(h->k1[v].as<float>(), vox(h->kd[v]), sum.as<double>(), s);
-    }
+    for (int v = 0; v < V; ++v) norm_kernel(h->k1[v].as<float>(), vox(h->kd[v]), sum.as<double>(), s);
   }
   // The plans of the PSF-pair convolutions (view v's PSF volume with view w's PSF) are built
   // here, with their tables uploaded in the handle stream's order, and each view gets scratch
@@ -607,11 +616,7 @@ void prepare_kernels(mvd_decon* h) {
     const long long nv = vox(dv);
     float* k2 = h->k2[v].as<float>();
     const float* k1 = h->k1[v].as<float>();
-    auto norm = [&](float* k) {
-      MVD_CHECK(cudaMemsetAsync(x.sum.p, 0, sizeof(double), st));
-      dev_sum_f64(k, nv, x.sum.as<double>(), st);
-      dev_scale_div(k, nv, x.sum.as<double>(), st);
-    };
+    auto norm = [&](float* k) { norm_kernel(k, nv, x.sum.as<double>(), st); };
     // out = ext0(in) (*) kern over in's dims
     auto conv0 = [&](const float* in, const float* kern, const std::array<int, 3>& kd, float* out) {
       ConvPlan& plan = plan_for(dv, kd);
@@ -778,6 +783,7 @@ extern "C" int mvd_create(mvd_decon** out, int devCUDA, const int* dims, int num
   h->psftype = psftype;
   h->lambda = (float)lambda;
   h->flags = flags;
+  h->ref_sum_threads = (int)(((unsigned)flags >> 16) & 0x7fffu);
   const size_t nb = h->N * sizeof(float);
   h->img.resize(num_views);
   h->w.resize(num_views);

@@ -37,6 +37,14 @@ FLAG_NO_GRAPH = 2
 FLAG_AUTOTUNE = 4
 
 
+def FLAG_REF_SUM_THREADS(threads: int) -> int:
+    """MVD_FLAG_REF_SUM_THREADS(t): normalise the kernels as AdjustInput.sumImg does with t
+    threads (portion 0 of divideIntoPortions(n, 2 t) counted twice, AdjustInput.java:114-118)."""
+    if not 1 <= int(threads) <= 32767:
+        raise ValueError("threads must be in [1, 32767]")
+    return int(threads) << 16
+
+
 class CUDAFourierConvolution:
     """The JNA interface bound to libFourierConvolutionCUDA (CUDAFourierConvolution.java:25-32)."""
 

@@ -102,6 +102,7 @@ def header_symbols() -> list[str]:
     path = os.path.join(os.path.dirname(_build.PKG), "include", "mvdecon.h")
     text = open(path).read()
     text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    text = re.sub(r"^[ \t]*#.*$", "", text, flags=re.M)  # preprocessor lines (function-like macros)
     names = re.findall(r"\b([A-Za-z_][A-Za-z0-9_]*)\s*\([^;{]*\)\s*;", text)
     return [n for n in names if n not in ("if", "while", "sizeof")]
 

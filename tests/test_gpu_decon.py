@@ -58,6 +58,26 @@ def test_deconvolution_matches_fp64_oracle(cfg, ptype):
         assert m == pytest.approx(rm, rel=1e-3, abs=1e-6)
 
 
+@pytest.mark.parametrize("threads", [1, 3])
+def test_reference_thread_count_normalisation(threads):
+    """MVD_FLAG_REF_SUM_THREADS(t) divides every kernel by its sum plus the sum of portion 0 of
+    divideIntoPortions(n, 2 t), as AdjustInput.sumImg does with t threads; the oracle's
+    quirk_threads restates it."""
+    from spim_registration_gb300 import FLAG_REF_SUM_THREADS
+
+    p = small(2, S.EFFICIENT_BAYESIAN, it=3)
+    ref, od = O.deconvolve(p, arith="f64", block=None, mask=False, quirk_threads=threads)
+    d = run_gpu(p, FLAG_REF_SUM_THREADS(threads))
+    for v in range(len(p.psfs)):
+        assert rel_max(d.kernel(v, 1), od.k1[v]) < 1e-6
+        assert rel_max(d.kernel(v, 2), od.k2[v]) < 1e-5
+        assert abs(float(d.kernel(v, 1).sum()) - 1.0) > 1e-3  # not a unit sum any more
+    got = d.get_psi()
+    assert rel_l2(got, ref) < RELL2, rel_l2(got, ref)
+    plain_sum = run_gpu(p).get_psi()
+    assert rel_l2(got, plain_sum) > 10 * RELL2  # the normalisation changes the result
+
+
 def test_no_tikhonov_and_ten_iterations():
     p = small(1, S.INDEPENDENT, it=10, lam=0.0)
     ref, _ = O.deconvolve(p, arith="f64", block=None, mask=False)
