@@ -77,6 +77,41 @@ def _blend_on_device(lib, torch, view_zyx, out_zyx, border, blend, offset=(0, 0,
     return oblend.cpu().numpy()
 
 
+@pytest.mark.parametrize("turn", ["x", "z"])
+def test_exact_quarter_turn_is_a_transpose(turn):
+    """A registration turning the view by exactly 90 degrees about y maps voxel centres onto
+    voxel centres, and the float inverse is exact: image and weight are the view's own values,
+    transposed and flipped, bit for bit.  The turn makes view x run along output z, which the
+    z-fast resampling kernel takes; "x" is the unturned view through the x-fast kernel."""
+    torch = pytest.importorskip("torch")
+    lib = native.load()
+    rng = np.random.default_rng(9)
+    sz, sy, sx = 37, 21, 45  # odd sizes: partial tiles in both kernels
+    view = (rng.random((sz, sy, sx)) * 100 + 1).astype(np.float32)
+    if turn == "z":
+        affine, out_shape = [0, 0, 1, 0, 0, 1, 0, 0, -1, 0, 0, sx - 1], (sx, sy, sz)
+        want = np.transpose(view, (2, 1, 0))[::-1]
+    else:
+        affine, out_shape = [1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0], (sz, sy, sx)
+        want = view
+    border, blend = (0.5, -2.0, 1.0), (9.0, 6.5, 7.25)
+    eye = [1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0]
+    w_view = O.transform_weights(view.shape, eye, (0, 0, 0), view.shape, border, blend)
+    want_w = np.transpose(w_view, (2, 1, 0))[::-1] if turn == "z" else w_view
+    dv = torch.from_numpy(view).cuda()
+    oimg = torch.full(out_shape, float("nan"), device="cuda")
+    oblend = torch.full(out_shape, float("nan"), device="cuda")
+    oz, oy, ox = out_shape
+    native.check(lib.mvd_transform_view(dv.data_ptr(), native.iarr([sx, sy, sz]),
+                                        (native.ctypes.c_double * 12)(*[float(a) for a in affine]),
+                                        native.iarr([0, 0, 0]), native.iarr([ox, oy, oz]), oimg.data_ptr(),
+                                        oblend.data_ptr(), (native.ctypes.c_float * 3)(*border),
+                                        (native.ctypes.c_float * 3)(*blend), 0, None))
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(oimg.cpu().numpy(), want)
+    np.testing.assert_array_equal(oblend.cpu().numpy(), want_w)
+
+
 def test_blending_weight_arithmetic_is_bit_exact():
     """With the identity registration the kernel and the oracle see the same float positions,
     so the weights must agree bit for bit: the lookup index (Math.round of the double product

@@ -211,6 +211,25 @@ def test_blend_table_follows_the_reference_fill_loop():
     assert np.all(np.diff(lut) >= 0)
 
 
+def test_transform_by_an_exact_quarter_turn_is_a_transpose():
+    """A registration that turns the view by exactly 90 degrees about y (integer matrix) maps
+    voxel centres onto voxel centres: the resampled view (TransformInput) and its blending weight
+    are the view's own values and weights, transposed and flipped."""
+    rng = np.random.default_rng(5)
+    sz, sy, sx = 5, 6, 7
+    view = (rng.random((sz, sy, sx)) * 10 + 1).astype(np.float32)
+    # view -> world: x_w = z_v, y_w = y_v, z_w = (sx - 1) - x_v
+    aff = [0, 0, 1, 0, 0, 1, 0, 0, -1, 0, 0, sx - 1]
+    out = O.transform_input(view, aff, (0, 0, 0), (sx, sy, sz))
+    want = np.transpose(view, (2, 1, 0))[::-1]  # out[z_w, y_w, x_w] = view[x_w, y_w, sx - 1 - z_w]
+    np.testing.assert_array_equal(out, want)
+    border, blend = (0.5, -2.0, 1.0), (3.0, 2.5, 2.0)
+    w_turned = O.transform_weights(view.shape, aff, (0, 0, 0), (sx, sy, sz), border, blend)
+    eye = [1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0]
+    w_view = O.transform_weights(view.shape, eye, (0, 0, 0), view.shape, border, blend)
+    np.testing.assert_array_equal(w_turned, np.transpose(w_view, (2, 1, 0))[::-1])
+
+
 def test_blending_weights_profile():
     # along x: 0 at the border, cosine ramp over `blending` voxels, 1 in the middle
     eye = [1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0]
