@@ -32,7 +32,7 @@ def _worker(rank, world, port, times, out):
 def test_two_gloo_replicas_take_the_slowest_rank():
     world = 2
     times = [40.0, 50.0]
-    with mp.Manager() as m:
+    with mp.get_context("spawn").Manager() as m:  # no fork from this multi-threaded process
         out = m.dict()
         mp.spawn(_worker, args=(world, _free_port(), times, out), nprocs=world, join=True)
         res = dict(out)
