@@ -145,7 +145,11 @@ def make_problem(workload):
 
 
 def bytes_per_iteration(dec, n_views, n_voxels):
-    """Algorithmic HBM bytes of one fused iteration per pass kind (byte model)."""
+    """Algorithmic HBM bytes of one fused iteration per pass kind, from the live tile plans.
+    Per view, with P the tile voxels, H the complex values of the tiles' half spectra and N the
+    volume's voxels: forward plane pass 4 P + 8 H and z pass 16 H + one OTF read, each twice
+    (two convolutions); inverse pass with the quotient 8 H_eff + 8 N; inverse pass with the
+    update 8 H_eff + 12 N."""
     out = {"plane_fwd": 0, "zpass": 0, "plane_inv_quotient": 0, "plane_inv_update": 0}
     for v in range(n_views):
         p = dec.plan(v)
