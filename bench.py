@@ -12,8 +12,8 @@ Arms:
                      MVDeconvolution / MVDeconFFT path, float32, scipy FFT on every core); the
                      reference's own Java code cannot run on this machine.
 
-Multi-GPU: the path does not shard across GPUs in this build (views are sequential, one GPU
-per box); with --gpus N each rank runs an independent replica on its own GPU ("weak" scaling,
+Multi-GPU: the path does not shard across GPUs (views are sequential, and the deployment is one
+GPU per machine); with --gpus N each rank runs an independent replica on its own GPU ("weak" scaling,
 value = all ranks' voxel-updates / max time over ranks).
 """
 from __future__ import annotations

@@ -1,7 +1,7 @@
 """CPU oracle for the multiview Bayesian deconvolution path.  TEST INFRASTRUCTURE ONLY.
 
 Only ``tests/``, ``__graft_entry__.smoke()`` and the CPU-baseline leg of ``bench.py`` use this
-module, as the checker or as the timed CPU restatement; the library never calls it.
+module, to check results or as the timed CPU restatement; the library never calls it.
 
 PARITY UNPINNED.  fiji/SPIM_Registration ships no tests, golden vectors or fixtures for this
 path, and the reference is Java (Maven, imglib2) with no JDK available to run it, so this file
@@ -585,7 +585,7 @@ def separable_convolve(image, kernels_xyz, oob, value=0.0):
     behaviour the interface documents (the native SeparableConvolutionCUDALib is an external
     project, not vendored): in place along x, then y, then z (a None kernel skips its axis);
     out[x] = sum_{j=-R..R} in[x + j] k[R - j]; each pass extends its own input (0 zero,
-    1 value, 2 border pixel) and is stored as float32.  FP64 accumulation (the checker)."""
+    1 value, 2 border pixel) and is stored as float32.  Accumulates in FP64."""
     out = np.asarray(image, dtype=np.float32)
     for axis_xyz, k in enumerate(kernels_xyz):
         if k is None:

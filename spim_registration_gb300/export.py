@@ -7,7 +7,7 @@ count, the display range and the calibration (the bounding box's origin divided 
 down-sampling, pixel size = the down-sampling, :99-113), or the same TIFF inside a ZIP archive
 (saveAsZip, :125-133).  This module writes that layout with numpy (no imaging library), and
 reads it back for checks.  The HDF5 / BigDataViewer export (ExportSpimData2HDF5) needs an HDF5
-library, which this build does not ship.
+library, which this package does not ship.
 """
 from __future__ import annotations
 
