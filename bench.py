@@ -1,9 +1,16 @@
 """Benchmark of the multiview deconvolution hot path: voxel-updates/s.
 
 One step = one deconvolution iteration (every view's conv1 -> quotient -> conv2 -> update) of
-the 4-view efficient-Bayesian workload 256x256x192, PSF 15x15x41 (sigma 1.5,1.5,5) rotated per
-view (0/45/90/135 deg about y), cosine-blended VIRTUAL weights; synthetic seeded inputs.
-voxel-updates/s = voxels * views * steps / time.
+the 4-view efficient-Bayesian workload 512x512x256, PSF 31x31x61 (sigma 2,2,7) rotated per view
+(0/45/90/135 deg about y, so the 45 and 135 degree views carry 65x31x65 PSFs), cosine-blended
+VIRTUAL weights; synthetic seeded inputs.  voxel-updates/s = voxels * views * steps / time.
+The 256x256x192 workload with 15x15x41 PSFs and 128^3 reference blocks is measured as well and
+reported in its own object (``workloads``).
+
+Besides the timed value the line carries the error of the timed handle's own tile plans against
+the FP64 oracle after 10 iterations (``accuracy_vs_fp64``, computed after the timed region), the
+plain FP32 form (the reference's block structure, one block per launch sequence), the e2e job
+through the C ABI from host buffers, and the CPU restatement timed on the host cores.
 
 Arms:
   (default)          the sm_103a library: fused tiled passes, all tiles of a view in one launch
@@ -40,7 +47,8 @@ WORKLOADS = {
     "cfg4_4view_eb_512x512x256": (4, (512, 512, 256), (31, 31, 61), None),
     "cfg1_2view_128x128x64": (1, (128, 128, 64), (9, 9, 25), None),
 }
-DEFAULT_WORKLOAD = "cfg2_4view_eb_256x256x192"
+DEFAULT_WORKLOAD = "cfg4_4view_eb_512x512x256"
+SECONDARY_WORKLOAD = "cfg2_4view_eb_256x256x192"  # reported beside the headline workload
 REFERENCE_MAX_SECONDS = 150.0  # bound on the reference arm's timed view stages
 
 
@@ -55,6 +63,8 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-autotune", action="store_true", help="planner's default tiles instead of timed ones")
+    ap.add_argument("--no-accuracy", action="store_true", help="skip the FP64 accuracy check")
+    ap.add_argument("--no-secondary", action="store_true", help="skip the 256x256x192 workload's object")
     ap.add_argument("--only", choices=["inputs", "separable"],
                     help="measure only the input preparation or the separable convolution at the workload's size")
     return ap.parse_args()
@@ -188,10 +198,79 @@ def replica_value(units_per_rank: float, ms_max: float, world: int) -> float:
     return units_per_rank * world / (ms_max / 1e3)
 
 
+def time_iterations(dec, stream, steps, world=1, clocks=None):
+    """CUDA-event time (ms) of `steps` iterations on the handle's stream, max over ranks; the
+    kernel launches issued meanwhile; the clock record if a sampler is given."""
+    import torch
+
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+    torch.cuda.synchronize()
+    if clocks is not None:
+        clocks.start()
+        time.sleep(0.3)  # let the sampler start before the timed region
+    launches0 = dec.launch_count()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        dec.run_iteration()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    clock_info = clocks.stop() if clocks is not None else None
+    return max_over_ranks(ms, world), dec.launch_count() - launches0, clock_info
+
+
+def accuracy_vs_fp64(dec, prob, device, iterations=10):
+    """Error of the handle's own tile plans against the FP64 oracle, after the timed region: psi
+    is reset to the first-iteration average, `iterations` iterations run, and the result is
+    compared with the oracle's float64 deconvolution of the same inputs (the oracle's torch
+    restatement on this GPU; the check, not the thing measured)."""
+    import torch
+
+    from oracle import fp64_torch as T
+
+    dec.set_psi(np.full(prob.views[0].shape, np.float32(dec.initial_average()), dtype=np.float32))
+    dec.run(iterations)
+    got = dec.get_psi()
+    got_masked = dec.get_psi(masked=True)
+    ref = T.Deconvolution(prob.views, prob.weights, prob.psfs, prob.psftype, prob.lam, device=f"cuda:{device}")
+    ref.run(iterations)
+    e = T.errors(got, ref.psi)
+    em = T.errors(got_masked, ref.masked_psi())
+    del ref
+    torch.cuda.empty_cache()
+    return {"iterations": iterations, "rel_l2": e["rel_l2"], "max_abs": e["max_abs"],
+            "max_abs_rel_to_max": e["max_abs_rel"], "rel_l2_masked": em["rel_l2"], "gate": 1e-4,
+            "passes": e["rel_l2"] <= 1e-4,
+            "oracle": "FP64 restatement of the reference loop (one whole-image block, float64 FFTs)"}
+
+
+def plain_form(prob, block, local, steps):
+    """The plain FP32 form: the reference's block structure (MVDeconFFT.java:128-165: the given
+    block size, or one block of image + kernel - 1), one block per launch sequence (copy, three
+    FFT passes, paste), separate quotient and update kernels, no graph."""
+    import torch
+
+    from spim_registration_gb300 import FLAG_PLAIN, Deconvolution
+
+    plain = Deconvolution(prob.views, prob.weights, prob.psfs, prob.psftype, prob.lam, local, FLAG_PLAIN, block)
+    pstream = torch.cuda.ExternalStream(plain.stream(), device=local)
+    plain.run_iteration()
+    plain.synchronize()
+    pms, _, _ = time_iterations(plain, pstream, steps)
+    psi = plain.get_psi()
+    plans = [plain.plan(v) for v in range(len(prob.views))]
+    plain.close()
+    return pms / steps, psi, plans
+
+
 def run_ours(args, rank, world, local):
     import torch
 
-    from spim_registration_gb300 import FLAG_AUTOTUNE, FLAG_PLAIN, Deconvolution
+    from spim_registration_gb300 import FLAG_AUTOTUNE, Deconvolution
     from spim_registration_gb300 import native
 
     torch.cuda.set_device(local)
@@ -210,36 +289,17 @@ def run_ours(args, rank, world, local):
         return {"workload": args.workload, key: fn(prob, local, hbm_peak)}
     n_vox = prob.n_voxels
     V = len(prob.views)
-    lib = native.load()
+    native.load()
 
-    dec = Deconvolution(prob.views, prob.weights, prob.psfs, prob.psftype, prob.lam, local,
-                        0 if args.no_autotune else FLAG_AUTOTUNE)
+    flags = 0 if args.no_autotune else FLAG_AUTOTUNE
+    dec = Deconvolution(prob.views, prob.weights, prob.psfs, prob.psftype, prob.lam, local, flags)
     stream = torch.cuda.ExternalStream(dec.stream(), device=local)
 
     # warm-up (captures the graph on the first iteration)
     for _ in range(args.warmup):
         dec.run_iteration()
     dec.synchronize()
-
-    if world > 1:
-        import torch.distributed as dist
-        dist.barrier()
-    torch.cuda.synchronize()
-    clocks = ClockSampler(local)
-    clocks.start()
-    time.sleep(0.3)  # let the sampler start before the timed region
-    launches0 = dec.launch_count()
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    for _ in range(args.steps):
-        dec.run_iteration()
-    e1.record(stream)
-    torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1)
-    clock_info = clocks.stop()
-    launches = dec.launch_count() - launches0
-    ms = max_over_ranks(ms, world)
+    ms, launches, clock_info = time_iterations(dec, stream, args.steps, world, ClockSampler(local))
     ms_per_step = ms / args.steps
     value = replica_value(n_vox * V * args.steps, ms, world)
 
@@ -259,6 +319,7 @@ def run_ours(args, rank, world, local):
             traffic = json.load(open(tpath)).get(args.workload, {}).get(dom)
         except Exception:
             traffic = None
+    plans = [dec.plan(v) for v in range(V)]
 
     out = {
         "metric": METRIC,
@@ -276,7 +337,7 @@ def run_ours(args, rank, world, local):
         "config": {"workload": args.workload, "views": V, "volume_xyz": list(prob.dims_xyz),
                    "psf_xyz": [list(p.shape[::-1]) for p in prob.psfs], "psftype": "EFFICIENT_BAYESIAN",
                    "lambda": prob.lam, "step": "one iteration over all views",
-                   "plans": [dec.plan(v) for v in range(V)], "flags": "planner default tiles" if args.no_autotune else "autotuned tile plans",
+                   "plans": plans, "flags": "planner default tiles" if args.no_autotune else "autotuned tile plans",
                    "l2": "working set per iteration > 129 MB L2 (no flush needed)",
                    "parallelism": f"replicas x{world}"},
         "gpu_launches": launches,
@@ -287,36 +348,25 @@ def run_ours(args, rank, world, local):
                      "algorithmic_bytes_per_launch": algo[dom] / max(dom_launches, 1),
                      "avg_launch_ms": dom_ms / max(dom_launches, 1), "traffic": traffic},
     }
+    if rank == 0 and not args.no_accuracy:
+        out["accuracy_vs_fp64"] = accuracy_vs_fp64(dec, prob, local, iterations=10)
     dec.close()
 
     if rank == 0 and not args.no_plain:
-        # the plain FP32 form: reference block structure, one block per launch sequence
         _, _, _, block = WORKLOADS[args.workload]
-        plain = Deconvolution(prob.views, prob.weights, prob.psfs, prob.psftype, prob.lam, local, FLAG_PLAIN, block)
-        pstream = torch.cuda.ExternalStream(plain.stream(), device=local)
-        plain.run_iteration()
-        plain.synchronize()
         psteps = max(1, min(3, args.steps))
-        a = torch.cuda.Event(enable_timing=True)
-        b = torch.cuda.Event(enable_timing=True)
-        torch.cuda.synchronize()
-        a.record(pstream)
-        for _ in range(psteps):
-            plain.run_iteration()
-        b.record(pstream)
-        torch.cuda.synchronize()
-        pms = a.elapsed_time(b) / psteps
+        pms, ppsi, pplans = plain_form(prob, block, local, psteps)
         pvalue = n_vox * V / (pms / 1e3)
-        # accuracy of the fused form against the plain form after the same iterations
+        # the fused form after the same iterations (1 + psteps), default plans
         fused = Deconvolution(prob.views, prob.weights, prob.psfs, prob.psftype, prob.lam, local, 0)
         fused.run(1 + psteps)
         f = fused.get_psi()
-        pl = plain.get_psi()
         fused.close()
-        plain.close()
-        out["plain_fp32_form"] = {"value": pvalue, "ms_per_step": pms, "block_xyz": block,
-                                  "speedup_of_value": value / world / pvalue,
-                                  "rel_l2_fused_vs_plain": float(np.linalg.norm(f - pl) / np.linalg.norm(pl))}
+        out["plain_fp32_form"] = {
+            "value": pvalue, "ms_per_step": pms, "steps": psteps,
+            "block_xyz": block if block is not None else "one block of image + kernel - 1 per view",
+            "plans": pplans, "speedup_of_value": value / world / pvalue,
+            "rel_l2_fused_vs_plain": float(np.linalg.norm(f - ppsi) / np.linalg.norm(ppsi))}
 
     if rank == 0 and not args.no_e2e:
         out["e2e"] = run_e2e(prob, local, steps=2)
@@ -325,7 +375,41 @@ def run_ours(args, rank, world, local):
         out["separable_convolution"] = run_separable(prob, local, hbm_peak)
     if rank == 0 and not args.no_cpu:
         out["cpu_baseline"] = cpu_baseline(prob)
+    if rank == 0 and not args.no_secondary and args.workload != SECONDARY_WORKLOAD:
+        del prob
+        out["workloads"] = {SECONDARY_WORKLOAD: run_secondary(SECONDARY_WORKLOAD, local, args)}
     return out
+
+
+def run_secondary(workload, local, args):
+    """The 256x256x192 workload (15x15x41 PSFs, the reference's 128^3 blocks for the plain form):
+    fused value with autotuned plans, the plain form's value and the FP64 error."""
+    import torch
+
+    from spim_registration_gb300 import FLAG_AUTOTUNE, Deconvolution
+
+    prob = make_problem(workload)
+    V, n_vox = len(prob.views), prob.n_voxels
+    dec = Deconvolution(prob.views, prob.weights, prob.psfs, prob.psftype, prob.lam, local,
+                        0 if args.no_autotune else FLAG_AUTOTUNE)
+    stream = torch.cuda.ExternalStream(dec.stream(), device=local)
+    for _ in range(5):
+        dec.run_iteration()
+    dec.synchronize()
+    steps = 100
+    ms, launches, _ = time_iterations(dec, stream, steps)
+    value = n_vox * V * steps / (ms / 1e3)
+    res = {"value": value, "unit": "voxel-updates/s", "ms_per_step": ms / steps, "steps": steps,
+           "gpu_launches": launches, "plans": [dec.plan(v) for v in range(V)]}
+    if not args.no_accuracy:
+        res["accuracy_vs_fp64"] = accuracy_vs_fp64(dec, prob, local, iterations=10)
+    dec.close()
+    if not args.no_plain:
+        block = WORKLOADS[workload][3]
+        pms, _, _ = plain_form(prob, block, local, 3)
+        res["plain_fp32_form"] = {"value": n_vox * V / (pms / 1e3), "ms_per_step": pms, "block_xyz": block,
+                                  "speedup_of_value": value / (n_vox * V / (pms / 1e3))}
+    return res
 
 
 def run_e2e(prob, device, steps=2):
@@ -491,11 +575,24 @@ def cpu_view_stage_time(prob, min_seconds=10.0, max_stages=64):
             return t / n, n, t
 
 
+def host_cores():
+    """Cores this process may run on (the GPU machine's host cores visible to it)."""
+    try:
+        return len(os.sched_getaffinity(0))
+    except Exception:
+        return os.cpu_count()
+
+
 def cpu_baseline(prob):
     per, n, total = cpu_view_stage_time(prob)
-    return {"value": prob.n_voxels / per, "unit": "voxel-updates/s", "cores": os.cpu_count(), "kind": "port",
-            "sample": f"{n} view stages (conv1, quotient, conv2, update) of the same workload, float32, "
-                      f"scipy.fft with {os.cpu_count()} workers; {total:.1f} s"}
+    return {"value": prob.n_voxels / per, "unit": "voxel-updates/s", "cores": host_cores(), "kind": "port",
+            "sample": f"{n} view stages (conv1, quotient, conv2, update) of the same workload, each convolution "
+                      f"over one whole-image block (the reference's single-block structure for this workload), "
+                      f"float32, scipy.fft with {_workers_note()}; {total:.1f} s"}
+
+
+def _workers_note():
+    return f"{os.cpu_count()} workers on the {host_cores()} host cores visible to this process"
 
 
 def run_reference(args, rank, world):
@@ -534,10 +631,11 @@ def run_reference(args, rank, world):
         "data": "synthetic (seeded blobs, Poisson noise, rotated Gaussian PSFs)",
         "config": {"workload": args.workload, "views": V, "volume_xyz": list(prob.dims_xyz),
                    "step": "one view stage (conv1, quotient, conv2, update) on the host cores"},
-        "cpu_baseline": {"value": value, "unit": "voxel-updates/s", "cores": os.cpu_count(), "kind": "port",
+        "cpu_baseline": {"value": value, "unit": "voxel-updates/s", "cores": host_cores(), "kind": "port",
                          "sample": f"{steps} view stages of the workload ({args.steps} asked, at most "
                                    f"{REFERENCE_MAX_SECONDS:.0f} s timed), CPU restatement of the Java "
-                                   "MVDeconvolution/MVDeconFFT loop (float32, scipy.fft on all cores); the Java "
+                                   "MVDeconvolution/MVDeconFFT loop (float32, one whole-image block per "
+                                   f"convolution, scipy.fft with {_workers_note()}); the Java "
                                    "reference needs a JDK and its Maven jars, absent on this machine"},
         "e2e": {"value": value, "unit": "voxel-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }

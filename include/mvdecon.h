@@ -98,11 +98,14 @@ int mvd_convolve3d_device(const float* in, float* out, const int* dims_xyz, cons
  * callers that may not call cudaMalloc / cudaFree while they run (a streaming acquisition
  * pipeline that cannot take an allocation's device-wide synchronisation, or a host framework
  * whose memory manager owns the device pool).  Same arguments and result as
- * mvd_convolve3d_device; all working memory comes from one static 64 MiB device array per GPU
- * (held until the process exits), and sizes whose plans, spectra and tables do not fit it are
- * rejected with MVD_ERR_ARG and a message.  The first call on a device looks the array up
- * (make it before any stream capture).  Calls share the array: calls that overlap on the GPU
- * race and must be serialised by the caller.  Returns after enqueueing on `stream`. */
+ * mvd_convolve3d_device, with two differences: stream == NULL means the legacy default stream
+ * (not the library's stream), and the call returns after enqueueing without waiting, so `out`
+ * is ready only once that stream's work is done.  All working memory comes from one static
+ * 64 MiB device array per GPU (held until the process exits), and sizes whose plans, spectra
+ * and tables do not fit it are rejected with MVD_ERR_ARG and a message.  The first call on a
+ * device looks the array up.  The call copies its small tables from host memory that is freed
+ * on return, so it is refused (MVD_ERR_STATE) while `stream` is being captured.  Calls share
+ * the array: calls that overlap on the GPU race and must be serialised by the caller. */
 int mvd_convolve3d_device_noalloc(const float* in, float* out, const int* dims_xyz, const float* kernel,
                                   const int* kdims_xyz, int ext_mode, float ext_value, int devCUDA,
                                   void* stream);

@@ -69,6 +69,7 @@ struct DeviceCtx {
   struct Otf {
     DevBuf buf;
     uint64_t stamp;
+    std::vector<float> kernel;  // the kernel's values: a hash match is confirmed against them
   };
   std::map<std::vector<uint64_t>, Otf> otfs;
   uint64_t clock = 0;
@@ -85,15 +86,19 @@ struct DeviceCtx {
   }
 
   // spectrum of a host kernel for a plan, cached by content (the Java side re-sends the same
-  // kernel with every block: MVDeconFFTThreads.java:86-89)
+  // kernel with every block: MVDeconFFTThreads.java:86-89).  The 64-bit hash only finds the
+  // entry; a hit is used only when the kept kernel values equal the new ones.
   const float2* otf_for(const ConvPlan& plan, const float* host_kernel) {
     const size_t kn = (size_t)plan.kx * plan.ky * plan.kz;
     std::vector<uint64_t> key{fnv1a(host_kernel, kn * sizeof(float)), (uint64_t)plan.kx, (uint64_t)plan.ky,
                               (uint64_t)plan.kz, (uint64_t)plan.ax.T, (uint64_t)plan.ay.T, (uint64_t)plan.az.T};
     auto it = otfs.find(key);
     if (it != otfs.end()) {
-      it->second.stamp = ++clock;
-      return it->second.buf.as<float2>();
+      if (std::memcmp(it->second.kernel.data(), host_kernel, kn * sizeof(float)) == 0) {
+        it->second.stamp = ++clock;
+        return it->second.buf.as<float2>();
+      }
+      otfs.erase(it);  // another kernel with the same hash: its spectrum is rebuilt below
     }
     if (otfs.size() >= 16) {  // evict the least recently used spectrum
       auto victim = otfs.begin();
@@ -107,6 +112,7 @@ struct DeviceCtx {
     o.buf.alloc(plan.otf_elems * sizeof(float2));
     build_otf(pt, plan, d_kernel.as<float>(), o.buf.as<float2>(), scratch, stream);
     o.stamp = ++clock;
+    o.kernel.assign(host_kernel, host_kernel + kn);
     auto& slot = otfs[key];
     slot = std::move(o);
     return slot.buf.as<float2>();

@@ -10,10 +10,12 @@
 // loads the library holds until the process exits.
 //
 // Set-up: the first call on a device (with that device current) looks up the array's device
-// address with cudaGetSymbolAddress and keeps it; that first call should come before any
-// stream capture.  Every call shares the array and its contents are whatever the last call
-// left there, so calls whose GPU work overlaps (another stream, another host thread) race on
-// it; callers serialise them.  The placed-kernel buffer is cleared on every call.
+// address with cudaGetSymbolAddress and keeps it.  Each call copies its plans and tables from
+// host vectors that are freed on return, so a call on a stream that is being captured is
+// refused.  A NULL stream is the legacy default stream, and the call returns once its work is
+// enqueued.  Every call shares the array and its contents are whatever the last call left
+// there, so calls whose GPU work overlaps (another stream, another host thread) race on it;
+// callers serialise them.  The placed-kernel buffer is cleared on every call.
 #include <cmath>
 #include <cstring>
 #include <mutex>
@@ -57,8 +59,8 @@ struct Axis {
   int T, n, E;
 };
 
-// tile choice: the smallest padded volume over smooth tile sizes whose planes fit the
-// kernels' shared-memory buffers (same rules as the allocating path's planner)
+// tile choice: the smallest padded volume over smooth tile sizes whose planes fit the plane
+// budget plane_cap() (the allocating path's planner and budget, so both pick the same tiles)
 std::vector<Axis> options(int size, int k, bool even, int tmax) {
   std::vector<Axis> out;
   int last = -1;
@@ -84,11 +86,6 @@ __global__ void place_kernel_noalloc(const float* __restrict__ k, int kx, int ky
     const int wz = ((z - kz / 2) % tz + tz) % tz;
     vol[((long long)wz * ty + wy) * tx + wx] = k[i];
   }
-}
-
-template <class K>
-void smem_attr(K kernel, size_t bytes) {
-  MVD_CHECK(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
 }
 
 }  // namespace
@@ -123,8 +120,16 @@ extern "C" int mvd_convolve3d_device_noalloc(const float* in, float* out, const 
       return MVD_ERR_ARG;
     }
     MVD_CHECK(cudaSetDevice(devCUDA));
-    unsigned char* base = scratch_address(devCUDA);
     cudaStream_t s = static_cast<cudaStream_t>(stream);
+    // the tables below are copied from host vectors that are freed on return: a graph captured
+    // from this call would read freed host memory, so a capturing stream is refused
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    MVD_CHECK(cudaStreamIsCapturing(s, &cap));
+    if (cap != cudaStreamCaptureStatusNone) {
+      set_last_error("mvd_convolve3d_device_noalloc cannot be called while its stream is being captured");
+      return MVD_ERR_STATE;
+    }
+    unsigned char* base = scratch_address(devCUDA);
 
     // ---- tile plan (host only) ----
     const int nx = dims[0], ny = dims[1], nz = dims[2];
@@ -135,7 +140,7 @@ extern "C" int mvd_convolve3d_device_noalloc(const float* in, float* out, const 
     Axis bx{}, by{}, bz{};
     for (auto& a : ox)
       for (auto& b : oy) {
-        if ((long long)row_pitch(a.T / 2) * b.T > kPlaneCap) continue;
+        if ((long long)row_pitch(a.T / 2) * b.T > plane_cap()) continue;
         for (auto& c : oz) {
           const double nt = (double)a.n * b.n * c.n;
           const double cost = nt * a.T * b.T * c.T * (1.0 + 1e-3 * nt);
@@ -269,12 +274,12 @@ extern "C" int mvd_convolve3d_device_noalloc(const float* in, float* out, const 
     MVD_CHECK(cudaGetLastError());
     EpiBoxes no_boxes;  // no L2 prefetch: no tensor maps are built on this path
     std::memset(&no_boxes, 0, sizeof(no_boxes));
-    smem_attr(plane_fwd_kernel<GatherValue>, smem_plane);
+    set_smem(plane_fwd_kernel<GatherValue>, smem_plane);
     plane_fwd_kernel<GatherValue><<<(int)otf_fwd.size(), kThreads, smem_plane, s>>>(
         d_tiles, reinterpret_cast<const int2*>(base + o_ofwd), d_plans, d_otf,
         GatherValue::full(d_place, bx.T, by.T, bz.T, 0.f), no_boxes, 0);
     MVD_CHECK(cudaGetLastError());
-    smem_attr(zpass_kernel<1>, smem_z);
+    set_smem(zpass_kernel<1>, smem_z);
     zpass_kernel<1><<<(int)otf_z.size(), kZThreads, smem_z, s>>>(d_tiles, reinterpret_cast<const int2*>(base + o_oz),
                                                                  d_plans, d_otf, nullptr,
                                                                  (float)(1.0 / ((double)bx.T * by.T * bz.T)));
@@ -283,7 +288,7 @@ extern "C" int mvd_convolve3d_device_noalloc(const float* in, float* out, const 
     // ---- the convolution: forward plane pass, z pass with the spectrum, inverse plane pass ----
     const int2* d_fwd = reinterpret_cast<const int2*>(base + o_fwd);
     if (ext_mode == 0) {
-      smem_attr(plane_fwd_kernel<GatherMirror>, smem_plane);
+      set_smem(plane_fwd_kernel<GatherMirror>, smem_plane);
       plane_fwd_kernel<GatherMirror><<<(int)fwd.size(), kThreads, smem_plane, s>>>(
           d_tiles, d_fwd, d_plans, d_spec, GatherMirror{{in, nx, ny, nz}}, no_boxes, 0);
     } else {
@@ -291,12 +296,12 @@ extern "C" int mvd_convolve3d_device_noalloc(const float* in, float* out, const 
           d_tiles, d_fwd, d_plans, d_spec, GatherValue::full(in, nx, ny, nz, ext_value), no_boxes, 0);
     }
     MVD_CHECK(cudaGetLastError());
-    smem_attr(zpass_kernel<0>, smem_z);
+    set_smem(zpass_kernel<0>, smem_z);
     zpass_kernel<0><<<(int)zz.size(), kZThreads, smem_z, s>>>(d_tiles, reinterpret_cast<const int2*>(base + o_z),
                                                               d_plans, d_spec, d_otf, 1.f);
     MVD_CHECK(cudaGetLastError());
     if (!inv.empty()) {
-      smem_attr(plane_inv_kernel<EpiStore>, smem_plane);
+      set_smem(plane_inv_kernel<EpiStore>, smem_plane);
       plane_inv_kernel<EpiStore><<<(int)inv.size(), kThreads, smem_plane, s>>>(
           d_tiles, reinterpret_cast<const int2*>(base + o_inv), d_plans, d_spec, EpiStore{out, nx, ny}, no_boxes);
       MVD_CHECK(cudaGetLastError());

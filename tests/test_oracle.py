@@ -271,3 +271,37 @@ def test_precomputed_weight_normalisation_and_overlap():
     # equal portions except the last one: the mean of portion means differs from the plain mean
     portions = O.divide_into_portions(cnt.size, 7)
     assert avg == pytest.approx(np.mean([cnt[s:s + l].mean() for s, l in portions]), rel=1e-12)
+
+
+@pytest.mark.parametrize("cfg,psftype,lam", [(2, O.EFFICIENT_BAYESIAN, 0.006), (1, O.INDEPENDENT, 0.0),
+                                             (2, O.OPTIMIZATION_I, 0.006)])
+def test_fp64_torch_restatement_matches_the_numpy_oracle(cfg, psftype, lam):
+    """The torch float64 restatement (the full-size checker) equals the numpy FP64 oracle on
+    the CPU: same kernels, same first iteration, same updates, to rounding."""
+    torch = pytest.importorskip("torch")
+    from oracle import fp64_torch as T
+
+    p = S.make_problem(cfg, shape_xyz=(30, 26, 22), psf_size_xyz=(7, 5, 9), n_blobs=8, iterations=2)
+    want = O.Deconvolution(p.views, p.weights, p.psfs, psftype, lam, "f64", None)
+    want.run(2)
+    got = T.Deconvolution(p.views, p.weights, p.psfs, psftype, lam, device="cpu")
+    got.run(2)
+    assert got.avg == pytest.approx(want.avg, rel=1e-13)
+    e = T.errors(torch.as_tensor(want.psi), got.psi)
+    assert e["rel_l2"] < 1e-12, e
+    for (_, _, s0, m0), (_, _, s1, m1) in zip(want.stats, got.stats):
+        assert s1 == pytest.approx(s0, rel=1e-9) and m1 == pytest.approx(m0, rel=1e-9)
+    np.testing.assert_allclose(got.masked_psi().numpy(), want.masked_psi(), rtol=1e-11, atol=1e-12)
+
+
+def test_fp64_torch_convolution_matches_direct_convolution():
+    torch = pytest.importorskip("torch")
+    from oracle import fp64_torch as T
+
+    r = rng(31)
+    img = r.random((9, 11, 13))
+    k = r.random((5, 3, 7))
+    for mode, value in ((O.MIRROR, 0.0), (O.VALUE, 1.0)):
+        c = T.Convolver(img.shape, k, "cpu")
+        got = c(torch.as_tensor(img), mode, value).numpy()
+        np.testing.assert_allclose(got, O.conv_direct(img, k, mode, value), rtol=1e-12, atol=1e-12)
