@@ -158,3 +158,18 @@ def errors(got, want: torch.Tensor) -> dict:
     max_abs = float(d.abs().max().item())
     return {"rel_l2": float(torch.linalg.vector_norm(d).item()) / max(norm, 1e-300), "max_abs": max_abs,
             "max_abs_rel": max_abs / max(mx, 1e-300)}
+
+
+def poisson_nll(psi, views, weights, psfs, device="cuda") -> float:
+    """``mvdecon_oracle.poisson_nll`` in float64 on ``device``: sum over views and voxels with
+    img > 0 of w (f - img log f), f = ext(psi) (*) P (mirror-single extension)."""
+    dd = dict(device=torch.device(device), dtype=torch.float64)
+    p = torch.as_tensor(np.asarray(psi, dtype=np.float64)).to(**dd)
+    total = 0.0
+    for img, w, k in zip(views, weights, psfs):
+        f = Convolver(p.shape, np.asarray(k, dtype=np.float64), dd["device"])(p, O.MIRROR)
+        im = torch.as_tensor(np.asarray(img, dtype=np.float32)).to(**dd)
+        wt = torch.as_tensor(np.asarray(w, dtype=np.float32)).to(**dd)
+        m = im > 0
+        total += float((wt[m] * (f[m] - im[m] * torch.log(f[m]))).sum().item())
+    return total

@@ -111,7 +111,7 @@ int next_smooth(int n, bool even) {
 }
 
 // Radices of the register DFTs (fft_device.cuh).
-static const int kRadices[] = {16, 15, 12, 10, 8, 6, 5, 4, 3, 2};
+static const int kRadices[] = {20, 18, 16, 15, 12, 10, 8, 6, 5, 4, 3, 2};
 
 static void best_split(int n, int depth, int maxdepth, std::vector<int>& cur, std::vector<int>& best) {
   if (n == 1) {
@@ -330,17 +330,6 @@ bool use_l2_prefetch() {
   static bool on = [] {
     const char* e = std::getenv("MVD_L2_PREFETCH");
     return !(e && e[0] == '0');
-  }();
-  return on;
-}
-
-// The slice-copy forward kernel is opt-in (MVD_TMA=1): with one slice per CTA the copy's latency
-// stands in front of all of the CTA's work, and on cfg2 it measured slower (0.735 vs 0.62 ms of
-// forward passes per iteration) than the gather that keeps ~20 loads per thread in flight.
-bool use_tma() {
-  static bool on = [] {
-    const char* e = std::getenv("MVD_TMA");
-    return e && e[0] == '1';
   }();
   return on;
 }

@@ -26,7 +26,7 @@ void check_cuda(cudaError_t e, const char* what);
 // 2,3,5-smooth helpers (the FFT radices are products of 2, 3 and 5)
 bool is_smooth(int n);
 int next_smooth(int n, bool even);
-std::vector<int> factorize(int n);  // radices from {16,15,12,10,8,6,5,4,3,2}, product == n
+std::vector<int> factorize(int n);  // radices from {20,18,16,15,12,10,8,6,5,4,3,2}, product == n
 
 // Device memory owned by RAII.  Allocated while an AllocScope is active on this thread, it
 // comes from the device's memory pool in the scope stream's order (cudaMallocAsync) and is
@@ -138,11 +138,6 @@ int plane_threads();
 bool use_fixed_planes();
 // L2 prefetch through tensor maps in the plane kernels (MVD_L2_PREFETCH=0 turns it off).
 bool use_l2_prefetch();
-// The TMA slice-copy forward kernel for compiled shapes (opt-in: MVD_TMA=1).
-bool use_tma();
-// Slice copies of the forward plane pass whose bounded wait gave up on the current device since
-// the last call (the counter is reset); 0 when the slice-copy kernel is off.
-int tma_timeouts();
 // Tensor map of a float volume [nz][ny][nx] with a (w, h, 1) box (cached); false when the volume
 // does not meet the tensor copy's rules (16-byte aligned base and row stride, box <= 256).
 bool volume_box_map(const float* base, int nx, int ny, int nz, int w, int h, CUtensorMap* out);

@@ -1,6 +1,6 @@
 // Large-radix Stockham FFT building blocks for sm_103a (FP32).
 //
-// A transform of length N = R_0 R_1 ... R_{S-1} (each R_s <= 16, S usually 2) runs as S
+// A transform of length N = R_0 R_1 ... R_{S-1} (each R_s <= 20, S usually 2) runs as S
 // stages.  In stage s every butterfly reads R_s values (stride N / R_s), twiddles them, runs
 // an R_s-point DFT in registers and writes them in Stockham (self-sorting) order.  Loads and
 // stores go through functors, so the first stage can read straight from global memory, the
@@ -31,7 +31,7 @@ constexpr int kMaxStages = 6;
 struct FftPlan {
   int n;                    // transform length
   int nstages;              // number of radix stages
-  int radix[kMaxStages];    // radices (each in {2,3,4,5,6,8,10,12,15,16}), product == n
+  int radix[kMaxStages];    // radices (each in {2,3,4,5,6,8,10,12,15,16,18,20}), product == n
   const float2* tw;         // exp(-2 pi i k / n), k in [0, n)
   const float2* tw_r2c;     // for the real-input length 2n: exp(-2 pi i k / (2n)), k in [0, n]
 };
@@ -221,6 +221,8 @@ template <bool INV> struct Dft<12, INV> : DftAB<4, 3, INV> {};
 template <bool INV> struct Dft<14, INV> : DftAB<2, 7, INV> {};
 template <bool INV> struct Dft<15, INV> : DftAB<3, 5, INV> {};
 template <bool INV> struct Dft<16, INV> : DftAB<4, 4, INV> {};
+template <bool INV> struct Dft<18, INV> : DftAB<2, 9, INV> {};
+template <bool INV> struct Dft<20, INV> : DftAB<4, 5, INV> {};
 
 // ---------------------------------------------------------------------------------------
 // butterfly index mapping
@@ -316,6 +318,8 @@ __device__ __forceinline__ void stage(int R, int N, int Ns, int count, const flo
     case 12: stage_r<12, INV, JFAST>(N, Ns, count, tw, ld, st); break;
     case 15: stage_r<15, INV, JFAST>(N, Ns, count, tw, ld, st); break;
     case 16: stage_r<16, INV, JFAST>(N, Ns, count, tw, ld, st); break;
+    case 18: stage_r<18, INV, JFAST>(N, Ns, count, tw, ld, st); break;
+    case 20: stage_r<20, INV, JFAST>(N, Ns, count, tw, ld, st); break;
     default: stage_r<1, INV, JFAST>(N, Ns, count, tw, ld, st); break;  // length-1 transform: copy
   }
 }
@@ -358,6 +362,8 @@ __device__ __forceinline__ void zmid(int R, int N, int count, const float2* __re
     case 12: zmid_r<12>(N, count, tw, ld, mul, st); break;
     case 15: zmid_r<15>(N, count, tw, ld, mul, st); break;
     case 16: zmid_r<16>(N, count, tw, ld, mul, st); break;
+    case 18: zmid_r<18>(N, count, tw, ld, mul, st); break;
+    case 20: zmid_r<20>(N, count, tw, ld, mul, st); break;
     default: zmid_r<1>(N, count, tw, ld, mul, st); break;
   }
 }

@@ -14,13 +14,13 @@
 namespace mvd {
 
 // The planner's factorisation (engine.cu factorize): fewest stages, then the largest smallest
-// radix, radices non-increasing, from {16, 15, 12, 10, 8, 6, 5, 4, 3, 2}.
+// radix, radices non-increasing, from {20, 18, 16, 15, 12, 10, 8, 6, 5, 4, 3, 2}.
 struct SplitC {
   int s = 0;
   int r[kMaxStages] = {0, 0, 0, 0, 0, 0};
 };
 
-constexpr int kRadixList[10] = {16, 15, 12, 10, 8, 6, 5, 4, 3, 2};
+constexpr int kRadixList[12] = {20, 18, 16, 15, 12, 10, 8, 6, 5, 4, 3, 2};
 
 __host__ __device__ constexpr int split_min(const SplitC& c) {
   int m = 1 << 30;
@@ -37,7 +37,7 @@ __host__ __device__ constexpr void split_search(int n, int depth, int maxdepth, 
     return;
   }
   if (depth == maxdepth) return;
-  for (int i = 0; i < 10; ++i) {
+  for (int i = 0; i < 12; ++i) {
     const int r = kRadixList[i];
     if (n % r) continue;
     if (cur.s && r > cur.r[cur.s - 1]) continue;
@@ -174,6 +174,12 @@ __device__ __forceinline__ void to_stages(int count, const float2* __restrict__ 
   }
 }
 
+// CTAs per SM the register allocation of a compiled-shape plane kernel is sized for: planes of
+// up to ~100 KB per buffer run 512-thread CTAs, two per SM (at most 64 registers a thread);
+// larger planes leave room for one CTA per SM, which then runs 1024 threads (also 64 registers)
+// so that twice as many warps hide the latency of the gathers and the shared-memory exchanges.
+__host__ __device__ constexpr int fixed_ctas_per_sm(int threads) { return threads >= 1024 ? 1 : 2; }
+
 // Forward plane pass: the generic kernel's structure (the first row stage gathers straight from
 // the volume, j-fastest) with the shape fixed.  Staging the slice in shared memory first, for
 // coalesced warp-per-row loads, measured slower on cfg2 (0.69 vs 0.64 ms per iteration): the
@@ -182,7 +188,7 @@ __device__ __forceinline__ void to_stages(int count, const float2* __restrict__ 
 // TY, 1) box; each CTA prefetches into L2 the slice of the CTA `ahead` launches later (one
 // resident wave on), so the next wave's gathers find their rows there.
 template <class Gather, int TX, int TY, int T>
-__global__ void __launch_bounds__(T, 2)
+__global__ void __launch_bounds__(T, fixed_ctas_per_sm(T))
 plane_fwd_fixed(const TileDesc* __restrict__ tiles, const int2* __restrict__ items, const FftPlan* __restrict__ plans,
                 float2* __restrict__ spec, Gather gather, const __grid_constant__ EpiBoxes src, int ahead) {
   constexpr int M = TX / 2, PX = M + 1, PITCH = row_pitch(M);
@@ -210,7 +216,7 @@ plane_fwd_fixed(const TileDesc* __restrict__ tiles, const int2* __restrict__ ite
 // effective rows stays in shared memory (batch-fastest stages), and the epilogue then walks the
 // effective region by whole warps per row: psi / weight / img accesses are fully coalesced.
 template <class Epi, int TX, int TY, int T>
-__global__ void __launch_bounds__(T, 2)
+__global__ void __launch_bounds__(T, fixed_ctas_per_sm(T))
 plane_inv_fixed(const TileDesc* __restrict__ tiles, const int2* __restrict__ items, const FftPlan* __restrict__ plans,
                 const float2* __restrict__ spec, Epi epi, const __grid_constant__ EpiBoxes boxes) {
   constexpr int M = TX / 2, PX = M + 1, PITCH = row_pitch(M);
@@ -350,18 +356,28 @@ zpass_fixed(const TileDesc* __restrict__ tiles, const int2* __restrict__ items, 
   }
 }
 
-// Pencil lengths with compiled z-pass kernels.
+// CTAs per SM a compiled z pass of length TZ is sized for: three when their shared memory (two
+// buffers of TZ x kZPitch complex each) fits, else two (with the registers two allow).
+__host__ __device__ constexpr int zpass_fixed_occ(int TZ) {
+  return 3 * 2 * TZ * kZPitch * 8 <= 227 * 1024 ? 3 : 2;
+}
+
+// Pencil lengths with compiled z-pass kernels: the 4-view 256x256x192 workload's (240, 216)
+// and the 512x512x256 workload's (320, 288).
 #define MVD_FIXED_Z_LENGTHS(X) \
   X(240)                       \
-  X(216)
+  X(216)                       \
+  X(320)                       \
+  X(288)
 
-// CTA size of the compiled-shape plane kernels (they replace the default 384-thread generic
-// kernels: a plan whose CTA size is the default runs them at this size).
-constexpr int kFixedThreads = 512;
-
-// Tile shapes (x length, y length) with compiled kernels.
+// Tile shapes (x length, y length, CTA size) with compiled kernels.  They replace the default
+// 384-thread generic kernels: a plan whose CTA size is the default runs them at their own size.
+// 100x100 and 128x100: the 256x256x192 workload's planes (two CTAs per SM); 160x160 and 192x96:
+// the 512x512x256 workload's (one CTA per SM).
 #define MVD_FIXED_PLANE_SHAPES(X) \
-  X(100, 100)                     \
-  X(128, 100)
+  X(100, 100, 512)                \
+  X(128, 100, 512)                \
+  X(160, 160, 1024)               \
+  X(192, 96, 1024)
 
 }  // namespace mvd

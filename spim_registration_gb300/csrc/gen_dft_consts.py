@@ -6,7 +6,7 @@ Run:  python spim_registration_gb300/csrc/gen_dft_consts.py
 import math
 import os
 
-SIZES = [6, 8, 9, 10, 12, 14, 15, 16]
+SIZES = [6, 8, 9, 10, 12, 14, 15, 16, 18, 20]
 out = ["// Generated by gen_dft_consts.py: W_R^m = exp(-2 pi i m / R) for composite R.",
        "#pragma once", "#include <cuda_runtime.h>", "", "namespace mvd {", ""]
 for r in SIZES:

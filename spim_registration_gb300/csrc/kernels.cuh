@@ -34,6 +34,10 @@ struct EpiBoxes {
   int count;
 };
 
+// Box width (floats) of a volume slice's L2 prefetch: a tile row of TX values at any x offset in
+// [0, 4) from the 16-byte boundary the box starts on, rounded up to 16 bytes.
+__host__ __device__ constexpr int prefetch_box_width(int TX) { return (TX + 3 + 3) / 4 * 4; }
+
 __device__ __forceinline__ void prefetch_box_l2(const CUtensorMap* map, int x, int y, int z) {
   asm volatile("cp.async.bulk.prefetch.tensor.3d.L2.global.tile [%0, {%1, %2, %3}];" ::"l"(
                    reinterpret_cast<uint64_t>(map)),

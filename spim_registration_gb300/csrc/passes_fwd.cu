@@ -10,68 +10,37 @@
 
 #include "engine.h"
 #include "fixed_plane.cuh"
-#include "tma_plane.cuh"
 
 namespace mvd {
 
 namespace {
 
-// CTAs of a plane kernel resident at once on the current device (two per SM)
-int resident_ctas() {
+// CTAs of a plane kernel resident at once on the current device
+int resident_ctas(int per_sm) {
   int dev = 0, sms = 0;
   MVD_CHECK(cudaGetDevice(&dev));
   MVD_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-  return 2 * sms;
-}
-
-// Per-device count of slice copies whose wait gave up (zero unless a copy never completed).
-int* tma_timeout_counter() {
-  static std::mutex mu;
-  static std::vector<int*> ptrs;
-  int dev = 0;
-  MVD_CHECK(cudaGetDevice(&dev));
-  std::lock_guard<std::mutex> lock(mu);
-  if ((int)ptrs.size() <= dev) ptrs.resize(dev + 1, nullptr);
-  if (!ptrs[dev]) {
-    MVD_CHECK(cudaMalloc(&ptrs[dev], sizeof(int)));
-    MVD_CHECK(cudaMemset(ptrs[dev], 0, sizeof(int)));
-  }
-  return ptrs[dev];
+  return per_sm * sms;
 }
 
 }  // namespace
 
-int tma_timeouts() {
-  if (!use_tma()) return 0;
-  int n = 0;
-  MVD_CHECK(cudaMemcpy(&n, tma_timeout_counter(), sizeof(int), cudaMemcpyDeviceToHost));
-  if (n) MVD_CHECK(cudaMemset(tma_timeout_counter(), 0, sizeof(int)));
-  return n;
-}
-
-// The compile-time-shaped kernel for (tx, ty) at 384 threads, if one is compiled.
+// The compile-time-shaped kernel for (tx, ty), if one is compiled (plans at the default CTA
+// size run it at its own size).
 template <class Gather>
 static bool launch_fwd_fixed(int tx, int ty, int threads, PlanTable& pt, const TileDesc* tiles, const int2* items,
                              int nitems, size_t smem, float2* spec, Gather g, cudaStream_t s) {
   if (threads != kThreads || !use_fixed_planes()) return false;
-#define MVD_FWD_CASE(TX, TY)                                                                              \
-  if (tx == TX && ty == TY) {                                                                             \
-    CUtensorMap map;                                                                                      \
-    if (use_tma() && volume_box_map(g.v.data, g.v.nx, g.v.ny, g.v.nz, tma_box_width(TX), TY, &map)) {     \
-      auto k = plane_fwd_tma<Gather, TX, TY, kFixedThreads>;                                              \
-      const size_t sm = tma_plane_smem<TX, TY>();                                                         \
-      set_smem(k, sm);                                                                                    \
-      k<<<nitems, kFixedThreads, sm, s>>>(tiles, items, pt.device(), spec, g, map, tma_timeout_counter()); \
-    } else {                                                                                              \
-      EpiBoxes src;                                                                                       \
-      std::memset(&src, 0, sizeof(src));                                                                  \
-      src.count = use_l2_prefetch() &&                                                                    \
-                  volume_box_map(g.v.data, g.v.nx, g.v.ny, g.v.nz, tma_box_width(TX), TY, &src.map[0]);   \
-      auto k = plane_fwd_fixed<Gather, TX, TY, kFixedThreads>;                                            \
-      set_smem(k, smem);                                                                                  \
-      k<<<nitems, kFixedThreads, smem, s>>>(tiles, items, pt.device(), spec, g, src, resident_ctas());    \
-    }                                                                                                     \
-    return true;                                                                                          \
+#define MVD_FWD_CASE(TX, TY, T)                                                                         \
+  if (tx == TX && ty == TY) {                                                                           \
+    EpiBoxes src;                                                                                       \
+    std::memset(&src, 0, sizeof(src));                                                                  \
+    src.count = use_l2_prefetch() &&                                                                    \
+                volume_box_map(g.v.data, g.v.nx, g.v.ny, g.v.nz, prefetch_box_width(TX), TY, &src.map[0]); \
+    auto k = plane_fwd_fixed<Gather, TX, TY, T>;                                                        \
+    set_smem(k, smem);                                                                                  \
+    k<<<nitems, T, smem, s>>>(tiles, items, pt.device(), spec, g, src, resident_ctas(fixed_ctas_per_sm(T))); \
+    return true;                                                                                        \
   }
   MVD_FIXED_PLANE_SHAPES(MVD_FWD_CASE)
 #undef MVD_FWD_CASE
@@ -87,10 +56,12 @@ static void launch_fwd_impl(PlanTable& pt, const TileDesc* tiles, const int2* it
     EpiBoxes src;
     std::memset(&src, 0, sizeof(src));
     src.count = !MASK && use_l2_prefetch() &&
-                volume_box_map(g.v.data, g.v.nx, g.v.ny, g.v.nz, tma_box_width(tx), ty, &src.map[0]);
+                volume_box_map(g.v.data, g.v.nx, g.v.ny, g.v.nz, prefetch_box_width(tx), ty, &src.map[0]);
     auto k = plane_fwd_kernel<Gather, MASK>;
     set_smem(k, smem);
-    k<<<nitems, threads > 0 ? threads : kThreads, smem, s>>>(tiles, items, pt.device(), spec, g, src, resident_ctas());
+    const int per_sm = 2 * smem <= 200 * 1024 ? 2 : 1;  // CTAs of this size an SM holds at once
+    k<<<nitems, threads > 0 ? threads : kThreads, smem, s>>>(tiles, items, pt.device(), spec, g, src,
+                                                             resident_ctas(per_sm));
   }
   MVD_CHECK(cudaGetLastError());
   count_launch();

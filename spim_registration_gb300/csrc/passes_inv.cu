@@ -21,7 +21,8 @@ static EpiBoxes epilogue_boxes(const ConvPlan& p, const Epi& e) {
   return b;
 }
 
-// The compile-time-shaped kernel for the plan's tile shape at 384 threads, if one is compiled.
+// The compile-time-shaped kernel for the plan's tile shape, if one is compiled (plans at the
+// default CTA size run it at its own size).
 template <class Epi>
 static bool launch_inv_fixed(PlanTable& pt, const ConvPlan& p, const TileDesc* tiles, const int2* items, int nitems,
                              const float2* spec, Epi e, cudaStream_t s) {
@@ -29,11 +30,11 @@ static bool launch_inv_fixed(PlanTable& pt, const ConvPlan& p, const TileDesc* t
   if (threads != kThreads || !use_fixed_planes()) return false;
   const int tx = p.ax.T, ty = p.ay.T;
   const EpiBoxes boxes = epilogue_boxes(p, e);
-#define MVD_INV_CASE(TX, TY)                                                           \
+#define MVD_INV_CASE(TX, TY, T)                                                        \
   if (tx == TX && ty == TY) {                                                          \
-    auto k = plane_inv_fixed<Epi, TX, TY, kFixedThreads>;                              \
+    auto k = plane_inv_fixed<Epi, TX, TY, T>;                                          \
     set_smem(k, p.smem_plane);                                                         \
-    k<<<nitems, kFixedThreads, p.smem_plane, s>>>(tiles, items, pt.device(), spec, e, boxes); \
+    k<<<nitems, T, p.smem_plane, s>>>(tiles, items, pt.device(), spec, e, boxes);      \
     return true;                                                                       \
   }
   MVD_FIXED_PLANE_SHAPES(MVD_INV_CASE)

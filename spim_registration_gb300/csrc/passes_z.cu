@@ -22,7 +22,7 @@ static bool launch_z_fixed(PlanTable& pt, const ConvPlan& p, float2* spec, const
   const int tz = p.az.T;
 #define MVD_Z_CASE(TZ)                                                                                       \
   if (tz == TZ) {                                                                                            \
-    auto k = zpass_fixed<TZ, 3>;                                                                             \
+    auto k = zpass_fixed<TZ, zpass_fixed_occ(TZ)>;                                                                           \
     set_smem(k, p.smem_z);                                                                                   \
     k<<<(int)p.items_z.size(), kZThreads, p.smem_z, s>>>(p.d_tiles.as<TileDesc>(), p.d_items_z.as<int2>(), \
                                                           pt.device(), spec, otf);                          \

@@ -22,7 +22,9 @@ SCRIPT = textwrap.dedent("""
     sys.path.insert(0, {root!r})
     from spim_registration_gb300 import Deconvolution
     from spim_registration_gb300 import synthetic as S
-    if sys.argv[2] == "full":
+    if sys.argv[2] == "large":  # the 512x512x256 workload's PSFs: 160x160 / 192x96 planes, 320 / 288 pencils
+        p = S.make_problem(4, shape_xyz=(260, 260, 256), psf_size_xyz=(31, 31, 61), n_blobs=60, iterations=1)
+    elif sys.argv[2] == "full":
         p = S.make_problem(2, shape_xyz=(172, 172, 192), psf_size_xyz=(15, 15, 41), n_blobs=40, iterations=2)
     else:  # data boxes smaller than the volume in x, y and z, still planned with 100/128-wide tiles
         p = S.make_problem(2, shape_xyz=(256, 256, 24), psf_size_xyz=(15, 15, 41), n_blobs=40, iterations=2)
@@ -36,8 +38,10 @@ SCRIPT = textwrap.dedent("""
 """)
 
 
-def _run(out, fixed, case="full", tma=False):
-    env = dict(os.environ, MVD_FIXED_PLANES="1" if fixed else "0", MVD_TMA="1" if tma else "0")
+def _run(out, fixed, case="full", cap=None):
+    env = dict(os.environ, MVD_FIXED_PLANES="1" if fixed else "0")
+    if cap:
+        env["MVD_PLANE_CAP"] = str(cap)
     r = subprocess.run([sys.executable, "-c", SCRIPT.format(root=ROOT), out, case], env=env, capture_output=True,
                        text=True, timeout=600)
     assert r.returncode == 0, r.stderr[-2000:]
@@ -53,12 +57,13 @@ def test_fixed_shape_kernels_equal_the_generic_kernels(tmp_path):
     np.testing.assert_array_equal(np.load(a), np.load(b))
 
 
-@pytest.mark.parametrize("case", ["full", "crop"])
-def test_slice_copy_forward_kernel_equals_the_generic_kernels(tmp_path, case):
-    """The opt-in TMA forward pass (MVD_TMA=1): its fix-up rewrites the mirror-single border and
-    the value outside data boxes smaller than the volume; psi must equal the generic path's."""
-    a, b = str(tmp_path / "tma.npy"), str(tmp_path / "generic.npy")
-    shapes = _run(a, True, case, tma=True)
-    assert _run(b, False, case) == shapes
-    assert any(t.startswith("100x100x") for t in shapes) and any(t.startswith("128x100x") for t in shapes)
+@pytest.mark.parametrize("cap,plane", [(14336, "160x160x"), (10240, "192x96x")])
+def test_large_psf_shapes_equal_the_generic_kernels(tmp_path, cap, plane):
+    """1024-thread compiled planes and the 320 / 288 compiled pencils (radices 20 and 18) of the
+    31x31x61-PSF workload against the generic kernels, bit for bit."""
+    a, b = str(tmp_path / "fixed.npy"), str(tmp_path / "generic.npy")
+    shapes = _run(a, True, "large", cap)
+    assert _run(b, False, "large", cap) == shapes
+    assert any(t.startswith(plane) for t in shapes), shapes
+    assert any(t.endswith("x320") for t in shapes) and (cap == 14336 or any(t.endswith("x288") for t in shapes))
     np.testing.assert_array_equal(np.load(a), np.load(b))

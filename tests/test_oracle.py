@@ -305,3 +305,34 @@ def test_fp64_torch_convolution_matches_direct_convolution():
         c = T.Convolver(img.shape, k, "cpu")
         got = c(torch.as_tensor(img), mode, value).numpy()
         np.testing.assert_allclose(got, O.conv_direct(img, k, mode, value), rtol=1e-12, atol=1e-12)
+
+
+def test_fp64_torch_nll_matches_the_numpy_oracle():
+    pytest.importorskip("torch")
+    from oracle import fp64_torch as T
+
+    p = S.make_problem(5, shape_xyz=(20, 18, 16), psf_size_xyz=(5, 5, 7), n_blobs=10, n_views=2, iterations=1)
+    psi = p.ground_truth.astype(np.float64) + 1.0
+    want = O.poisson_nll(psi, p.views, p.weights, p.psfs)
+    assert T.poisson_nll(psi, p.views, p.weights, p.psfs, device="cpu") == pytest.approx(want, rel=1e-12)
+
+
+def test_simplex_projection():
+    from spim_registration_gb300.psf_refine import project_simplex
+
+    r = rng(41)
+    for shape in ((7,), (3, 5, 7)):
+        x = r.normal(size=shape) * 0.3
+        p = project_simplex(x)
+        assert p.shape == x.shape and np.all(p >= 0) and p.sum() == pytest.approx(1.0, abs=1e-12)
+        # the projection is the closest simplex point: moving mass between two entries never helps
+        for _ in range(50):
+            i, j = r.integers(0, x.size, 2)
+            t = min(1e-3, p.flat[i])
+            q = p.copy()
+            q.flat[i] -= t
+            q.flat[j] += t
+            assert np.sum((q - x) ** 2) >= np.sum((p - x) ** 2) - 1e-15
+    y = np.abs(r.random(10))
+    y /= y.sum()
+    np.testing.assert_allclose(project_simplex(y), y, atol=1e-15)  # points of the simplex stay put
