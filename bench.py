@@ -4,8 +4,9 @@ One step = one deconvolution iteration (every view's conv1 -> quotient -> conv2 
 the 4-view efficient-Bayesian workload 512x512x256, PSF 31x31x61 (sigma 2,2,7) rotated per view
 (0/45/90/135 deg about y, so the 45 and 135 degree views carry 65x31x65 PSFs), cosine-blended
 VIRTUAL weights; synthetic seeded inputs.  voxel-updates/s = voxels * views * steps / time.
-The 256x256x192 workload with 15x15x41 PSFs and 128^3 reference blocks is measured as well and
-reported in its own object (``workloads``).
+The 4-view 256x256x192 workload and the 6-view workload cropped to random boxes in a 256^3
+volume (15x15x41 PSFs, 128^3 reference blocks) are measured as well, each in its own object
+(``workloads``); so is the same workload with the tensor-core DFT stages (``tensor_dft``).
 
 Besides the timed value the line carries the error of the timed handle's own tile plans against
 the FP64 oracle after 10 iterations (``accuracy_vs_fp64``, computed after the timed region), the
@@ -48,7 +49,8 @@ WORKLOADS = {
     "cfg1_2view_128x128x64": (1, (128, 128, 64), (9, 9, 25), None),
 }
 DEFAULT_WORKLOAD = "cfg4_4view_eb_512x512x256"
-SECONDARY_WORKLOAD = "cfg2_4view_eb_256x256x192"  # reported beside the headline workload
+# reported beside the headline workload, each in its own object
+SECONDARY_WORKLOADS = ("cfg2_4view_eb_256x256x192", "cfg3_6view_crops_256")
 REFERENCE_MAX_SECONDS = 150.0  # bound on the reference arm's timed view stages
 
 
@@ -64,8 +66,11 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-autotune", action="store_true", help="planner's default tiles instead of timed ones")
     ap.add_argument("--no-accuracy", action="store_true", help="skip the FP64 accuracy check")
-    ap.add_argument("--no-secondary", action="store_true", help="skip the 256x256x192 workload's object")
+    ap.add_argument("--no-secondary", action="store_true", help="skip the other workloads' objects")
     ap.add_argument("--no-psf-refine", action="store_true", help="skip the PSF refinement object")
+    ap.add_argument("--no-tensor-dft", action="store_true", help="skip the tensor-core DFT stage object")
+    ap.add_argument("--tensor-dft", action="store_true",
+                    help="time the handle with the tensor-core middle DFT stages as the line's value")
     ap.add_argument("--only", choices=["inputs", "separable"],
                     help="measure only the input preparation or the separable convolution at the workload's size")
     return ap.parse_args()
@@ -271,7 +276,7 @@ def plain_form(prob, block, local, steps):
 def run_ours(args, rank, world, local):
     import torch
 
-    from spim_registration_gb300 import FLAG_AUTOTUNE, Deconvolution
+    from spim_registration_gb300 import FLAG_AUTOTUNE, FLAG_TENSOR_DFT, Deconvolution
     from spim_registration_gb300 import native
 
     torch.cuda.set_device(local)
@@ -292,7 +297,7 @@ def run_ours(args, rank, world, local):
     V = len(prob.views)
     native.load()
 
-    flags = 0 if args.no_autotune else FLAG_AUTOTUNE
+    flags = (0 if args.no_autotune else FLAG_AUTOTUNE) | (FLAG_TENSOR_DFT if args.tensor_dft else 0)
     dec = Deconvolution(prob.views, prob.weights, prob.psfs, prob.psftype, prob.lam, local, flags)
     stream = torch.cuda.ExternalStream(dec.stream(), device=local)
 
@@ -349,9 +354,13 @@ def run_ours(args, rank, world, local):
                      "algorithmic_bytes_per_launch": algo[dom] / max(dom_launches, 1),
                      "avg_launch_ms": dom_ms / max(dom_launches, 1), "traffic": traffic},
     }
+    if args.tensor_dft:
+        out["config"]["flags"] += ", middle DFT stages of the 320 / 288 z passes on the tensor cores"
     if rank == 0 and not args.no_accuracy:
         out["accuracy_vs_fp64"] = accuracy_vs_fp64(dec, prob, local, iterations=10)
     dec.close()
+    if rank == 0 and not args.no_tensor_dft and not args.tensor_dft:
+        out["tensor_dft"] = run_tensor_dft(prob, local, flags, value, args)
 
     if rank == 0 and not args.no_plain:
         _, _, _, block = WORKLOADS[args.workload]
@@ -378,10 +387,52 @@ def run_ours(args, rank, world, local):
         out["cpu_baseline"] = cpu_baseline(prob)
     if rank == 0 and not args.no_psf_refine:
         out["psf_refinement"] = run_psf_refinement(local)
-    if rank == 0 and not args.no_secondary and args.workload != SECONDARY_WORKLOAD:
+    if rank == 0 and not args.no_secondary:
         del prob
-        out["workloads"] = {SECONDARY_WORKLOAD: run_secondary(SECONDARY_WORKLOAD, local, args)}
+        out["workloads"] = {w: run_secondary(w, local, args) for w in SECONDARY_WORKLOADS if w != args.workload}
     return out
+
+
+def run_tensor_dft(prob, local, flags, simt_value, args, steps=50):
+    """The same workload with the middle 16-point DFTs of the 320- and 288-long z passes on the
+    tensor cores (tcgen05 TF32 products, three-term hi/lo split, FP32 accumulation): its value,
+    and its error against the FP64 oracle after 10 and 50 iterations (relative L2 and max-abs of
+    the output volume, psi)."""
+    import torch
+
+    from spim_registration_gb300 import FLAG_TENSOR_DFT, Deconvolution
+
+    V, n_vox = len(prob.views), prob.n_voxels
+    dec = Deconvolution(prob.views, prob.weights, prob.psfs, prob.psftype, prob.lam, local, flags | FLAG_TENSOR_DFT)
+    stream = torch.cuda.ExternalStream(dec.stream(), device=local)
+    for _ in range(3):
+        dec.run_iteration()
+    dec.synchronize()
+    ms, launches, _ = time_iterations(dec, stream, steps)
+    dec.synchronize()  # reports any tensor-core stage whose bounded wait gave up
+    value = n_vox * V * steps / (ms / 1e3)
+    prof = dec.profile_iteration()
+    res = {"value": value, "unit": "voxel-updates/s", "ms_per_step": ms / steps, "steps": steps,
+           "value_over_fp32_simt": value / simt_value, "zpass_ms": prof["zpass"][0],
+           "plans": [dec.plan(v) for v in range(V)]}
+    if not args.no_accuracy:
+        from oracle import fp64_torch as T
+
+        dec.set_psi(np.full(prob.views[0].shape, np.float32(dec.initial_average()), dtype=np.float32))
+        ref = T.Deconvolution(prob.views, prob.weights, prob.psfs, prob.psftype, prob.lam, device=f"cuda:{local}")
+        done = 0
+        for it in (10, 50):
+            dec.run(it - done)
+            ref.run(it - done)
+            done = it
+            e = T.errors(dec.get_psi(), ref.psi)
+            res[f"accuracy_vs_fp64_{it}_iterations"] = {"rel_l2": e["rel_l2"], "max_abs": e["max_abs"],
+                                                        "max_abs_rel_to_max": e["max_abs_rel"]}
+        dec.synchronize()
+        del ref
+        torch.cuda.empty_cache()
+    dec.close()
+    return res
 
 
 def run_psf_refinement(local, steps=10):
@@ -423,8 +474,10 @@ def run_psf_refinement(local, steps=10):
 
 
 def run_secondary(workload, local, args):
-    """The 256x256x192 workload (15x15x41 PSFs, the reference's 128^3 blocks for the plain form):
-    fused value with autotuned plans, the plain form's value and the FP64 error."""
+    """Another workload (15x15x41 PSFs, the reference's 128^3 blocks for the plain form): the
+    4-view 256x256x192 one, or six views cropped to random boxes in a 256^3 volume (uneven tile
+    grids per view); fused value with autotuned plans, the plain form's value and the FP64
+    error."""
     import torch
 
     from spim_registration_gb300 import FLAG_AUTOTUNE, Deconvolution

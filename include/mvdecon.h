@@ -67,7 +67,10 @@ enum {
   MVD_FLAG_PLAIN = 1,    /* reference structure: one block per launch sequence, separate
                             quotient / update kernels, no graph (the plain FP32 GPU form) */
   MVD_FLAG_NO_GRAPH = 2, /* batched, fused passes but launched eagerly (no CUDA graph) */
-  MVD_FLAG_AUTOTUNE = 4  /* time candidate tile plans per view at creation and keep the fastest */
+  MVD_FLAG_AUTOTUNE = 4, /* time candidate tile plans per view at creation and keep the fastest */
+  MVD_FLAG_TENSOR_DFT = 8 /* z passes of the compiled pencil lengths 320 and 288 run their middle
+                             16-point DFTs on the tensor cores (TF32, three-term split, FP32
+                             accumulation); other lengths stay on the FP32 SIMT path */
 };
 
 /* AdjustInput.sumImg's dependence on the thread count (AdjustInput.java:114-118): the Java code
@@ -155,6 +158,12 @@ int mvd_get_iteration(mvd_decon* h, int* iteration);
 int mvd_get_plan(mvd_decon* h, int view, int* tiles_xyz, int* tile_xyz, int* eff_xyz,
                  long long* padded_voxels);
 
+/* The kernels the view's plan runs (chosen by MVD_FLAG_AUTOTUNE, else the defaults): *threads =
+ * the plane kernels' CTA size; *variant bit 0 = compile-time-shaped kernels, bit 1 = radices in
+ * ascending order (generic kernels), bit 2 = tensor-core middle DFT stage in the z pass.  No
+ * counterpart in the reference. */
+int mvd_get_plan_variant(mvd_decon* h, int view, int* threads, int* variant);
+
 /* The cudaStream_t the handle enqueues on (for events recorded by the caller). */
 int mvd_get_stream(mvd_decon* h, void** stream);
 
@@ -163,8 +172,9 @@ int mvd_get_launch_count(mvd_decon* h, long long* launches);
 
 /* Runs one iteration eagerly with CUDA events around each pass and returns the summed
  * device time per pass kind in milliseconds: ms[0] forward plane passes, ms[1] z passes,
- * ms[2] inverse plane + quotient, ms[3] inverse plane + update, ms[4] everything else;
- * launches[k] the number of launches of each kind. */
+ * ms[2] inverse plane + quotient, ms[3] inverse plane + update (whose last CTA also files the
+ * view's statistics), ms[4] everything else (nothing in the fused form); launches[k] the number
+ * of launches of each kind. */
 int mvd_profile_iteration(mvd_decon* h, double* ms, int* launches);
 
 /* ----- forward / backward of the multiview Poisson image-formation model -----

@@ -9,6 +9,7 @@ from .mvdecon import (  # noqa: F401
     FLAG_NO_GRAPH,
     FLAG_PLAIN,
     FLAG_REF_SUM_THREADS,
+    FLAG_TENSOR_DFT,
     PSFTYPE,
     CUDAFourierConvolution,
     Deconvolution,

@@ -359,12 +359,13 @@ constexpr int kHist = 64;
 struct StatSlot {
   double sum;
   unsigned max_bits;
-  unsigned pad;
+  unsigned ticket;  // CTAs of the view's update pass that are done (the last one archives)
 };
 
 // Copies the view's statistics into the history and clears its slot for the view's next
-// update (the slots start cleared); after the last view the iteration counter advances.  This
-// keeps a view's bookkeeping to one small node in the iteration graph.
+// update (the slots start cleared); after the last view the iteration counter advances.  The
+// plain form runs it after its separate update kernel; the fused update pass does the same in
+// its last CTA.
 __global__ void archive_stats_kernel(StatSlot* slot, double* hist, int* iter, int view, int nviews) {
   const int it = *iter % kHist;
   hist[(it * nviews + view) * 2 + 0] = slot->sum;
@@ -472,11 +473,14 @@ struct mvd_decon {
       launch_inv_quotient(pt, p, sp, img[v].as<float>(), q.as<float>(), s);
       launch_fwd_value(pt, p, q.as<float>(), 1.f, sp, s);
       launch_z(pt, p, sp, otf2[v].as<float2>(), s);
-      launch_inv_update(pt, p, sp, psi.as<float>(), w[v].as<float>(), lambda, &slot(v)->sum, &slot(v)->max_bits, s);
+      launch_inv_update(pt, p, sp, psi.as<float>(), w[v].as<float>(), lambda, &slot(v)->sum, &slot(v)->max_bits,
+                        archive(v), s);
     }
-    archive_stats_kernel<<<1, 1, 0, s>>>(slot(v), hist.as<double>(), d_iter.as<int>(), v, V);
-    MVD_CHECK(cudaGetLastError());
-    count_launch();
+  }
+
+  // the update pass's last CTA files view v's statistics (fused form)
+  StatArchive archive(int v) {
+    return StatArchive{hist.as<double>(), d_iter.as<int>(), &slot(v)->ticket, v, V, kHist};
   }
 
   // one block per launch sequence: copy block -> 3 FFT passes -> paste (MVDeconFFT.java:438-446,
@@ -499,6 +503,9 @@ struct mvd_decon {
     plain_conv(v, q.as<float>(), Ext::Value, 1.f, otf2[v].as<float2>(), tmp2.as<float>());
     dev_update(psi.as<float>(), tmp2.as<float>(), w[v].as<float>(), lambda, N, &slot(v)->sum, &slot(v)->max_bits,
                stream);
+    archive_stats_kernel<<<1, 1, 0, stream>>>(slot(v), hist.as<double>(), d_iter.as<int>(), v, V);
+    MVD_CHECK(cudaGetLastError());
+    count_launch();
   }
 
   void enqueue_iteration() {
@@ -676,64 +683,90 @@ void prepare_kernels(mvd_decon* h) {
 // 384- and 256-thread plane CTAs, are all tried and the fastest plan (one timed view stage
 // each) is kept.  More warps hide more latency; fewer threads leave fewer idle at the stages'
 // last butterfly round, which wins for some plane shapes.
-std::unique_ptr<ConvPlan> plan_view(mvd_decon* h, int v, const int lo[3], const int hi[3], bool autotune) {
+std::unique_ptr<ConvPlan> plan_view(mvd_decon* h, int v, const int lo[3], const int hi[3], bool autotune,
+                                    bool tensor_dft) {
   const auto& k = h->kd[v];
   const int n[3] = {hi[0] - lo[0], hi[1] - lo[1], hi[2] - lo[2]};
   const bool full = lo[0] == 0 && lo[1] == 0 && lo[2] == 0 && hi[0] == h->dims[0] && hi[1] == h->dims[1] &&
                     hi[2] == h->dims[2];
-  auto make = [&](int cap) {
+  auto make = [&](int cap, bool ascending) {
     PlanOptions o;
     o.cap = cap;
+    o.ascending = ascending;
     auto p = make_conv_plan(h->pt, n[0], n[1], n[2], k[0], k[1], k[2], o);
     if (!full) place_plan(*p, lo[0], lo[1], lo[2], h->dims);
+    p->tensor_dft = tensor_dft;
     return p;
   };
-  if (!autotune) return make(0);
+  if (!autotune) return make(0, false);
+  // one view stage of a candidate (two convolutions' passes), best of 3 after a warm-up
+  cudaEvent_t e0, e1;
+  MVD_CHECK(cudaEventCreate(&e0));
+  MVD_CHECK(cudaEventCreate(&e1));
+  auto time_stage = [&](ConvPlan& p, DevBuf& otf, DevBuf& spec) {
+    float ms = 1e30f;
+    for (int rep = 0; rep < 4; ++rep) {
+      MVD_CHECK(cudaEventRecord(e0, h->stream));
+      launch_fwd_mirror(h->pt, p, h->psi.as<float>(), spec.as<float2>(), h->stream);
+      launch_z(h->pt, p, spec.as<float2>(), otf.as<float2>(), h->stream);
+      launch_inv_quotient(h->pt, p, spec.as<float2>(), h->img[v].as<float>(), h->q.as<float>(), h->stream);
+      launch_fwd_value(h->pt, p, h->q.as<float>(), 1.f, spec.as<float2>(), h->stream);
+      launch_z(h->pt, p, spec.as<float2>(), otf.as<float2>(), h->stream);
+      launch_inv_quotient(h->pt, p, spec.as<float2>(), h->img[v].as<float>(), h->q.as<float>(), h->stream);
+      MVD_CHECK(cudaEventRecord(e1, h->stream));
+      MVD_CHECK(cudaEventSynchronize(e1));
+      float t = 0.f;
+      MVD_CHECK(cudaEventElapsedTime(&t, e0, e1));
+      if (rep > 0) ms = std::min(ms, t);
+    }
+    return ms;
+  };
+  // Candidates: the tile shapes of four plane budgets; for each, the default kernels (the
+  // compiled ones where the shape has them), the generic kernels at 384 threads (where compiled
+  // ones exist) and at 256 threads, and the generic kernels with every length's radices in
+  // ascending order (a second radix plan of the same lengths).
   std::unique_ptr<ConvPlan> best;
   float best_ms = 1e30f;
   std::vector<std::array<int, 3>> seen;
   for (int cap : {4608, 7168, 10240, 14336}) {
-    auto p = make(cap);
+    auto p = make(cap, false);
     const std::array<int, 3> shape{p->ax.T, p->ay.T, p->az.T};
     if (std::find(seen.begin(), seen.end(), shape) != seen.end()) continue;
     seen.push_back(shape);
     DevBuf otf(p->otf_elems * sizeof(float2)), spec(p->spec_elems * sizeof(float2));
     MVD_CHECK(cudaMemsetAsync(otf.p, 0, otf.bytes, h->stream));
-    cudaEvent_t e0, e1;
-    MVD_CHECK(cudaEventCreate(&e0));
-    MVD_CHECK(cudaEventCreate(&e1));
+    struct Variant {
+      int threads;
+      bool generic;
+    };
+    std::vector<Variant> variants{{kThreads, false}, {256, true}};
+    if (has_compiled_kernels(*p)) variants.push_back({kThreads, true});
     float ms = 1e30f;
-    int best_threads = kThreads;
-    for (int threads : {kThreads, 256}) {
-      p->threads_plane = threads;
-      float ms_t = 1e30f;
-      for (int rep = 0; rep < 4; ++rep) {  // rep 0 warms up
-        MVD_CHECK(cudaEventRecord(e0, h->stream));
-        launch_fwd_mirror(h->pt, *p, h->psi.as<float>(), spec.as<float2>(), h->stream);
-        launch_z(h->pt, *p, spec.as<float2>(), otf.as<float2>(), h->stream);
-        launch_inv_quotient(h->pt, *p, spec.as<float2>(), h->img[v].as<float>(), h->q.as<float>(), h->stream);
-        launch_fwd_value(h->pt, *p, h->q.as<float>(), 1.f, spec.as<float2>(), h->stream);
-        launch_z(h->pt, *p, spec.as<float2>(), otf.as<float2>(), h->stream);
-        launch_inv_quotient(h->pt, *p, spec.as<float2>(), h->img[v].as<float>(), h->q.as<float>(), h->stream);
-        MVD_CHECK(cudaEventRecord(e1, h->stream));
-        MVD_CHECK(cudaEventSynchronize(e1));
-        float t = 0.f;
-        MVD_CHECK(cudaEventElapsedTime(&t, e0, e1));
-        if (rep > 0) ms_t = std::min(ms_t, t);
-      }
-      if (ms_t < ms) {
-        ms = ms_t;
-        best_threads = threads;
+    Variant bv = variants[0];
+    for (const Variant& var : variants) {
+      p->threads_plane = var.threads;
+      p->generic = var.generic;
+      const float t = time_stage(*p, otf, spec);
+      if (t < ms) {
+        ms = t;
+        bv = var;
       }
     }
-    p->threads_plane = best_threads;
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
+    p->threads_plane = bv.threads;
+    p->generic = bv.generic;
+    auto asc = make(cap, true);
+    const float t_asc = time_stage(*asc, otf, spec);
+    if (t_asc < ms) {
+      ms = t_asc;
+      p = std::move(asc);
+    }
     if (ms < best_ms) {
       best_ms = ms;
       best = std::move(p);
     }
   }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
   return best;
 }
 
@@ -869,7 +902,9 @@ extern "C" int mvd_create(mvd_decon** out, int devCUDA, const int* dims, int num
         lo[d] = empty ? 0 : b[d];
         hi[d] = empty ? dims[d] : b[3 + d] + 1;
       }
-      h->plans.push_back(plan_view(h.get(), v, lo, hi, (flags & MVD_FLAG_AUTOTUNE) != 0));
+      if (flags & MVD_FLAG_TENSOR_DFT) tensor_dft_prepare();
+      h->plans.push_back(plan_view(h.get(), v, lo, hi, (flags & MVD_FLAG_AUTOTUNE) != 0,
+                                   (flags & MVD_FLAG_TENSOR_DFT) != 0));
       // the view's kernel spectra run on the GPU while the host plans the next view
       build_view_otfs(h.get(), v);
     }
@@ -949,6 +984,10 @@ extern "C" int mvd_synchronize(mvd_decon* h) {
   if (!h) return fail(MVD_ERR_ARG, "NULL handle");
   MVD_CHECK(cudaSetDevice(h->dev));
   MVD_CHECK(cudaStreamSynchronize(h->stream));
+  // a tensor-core z pass whose bounded wait gave up left its CTA's pencils uncomputed
+  if (h->flags & MVD_FLAG_TENSOR_DFT)
+    if (const int n = tensor_dft_failures())
+      return fail(MVD_ERR_CUDA, std::to_string(n) + " tensor-core DFT stages gave up waiting for their products");
   return MVD_OK;
   MVD_API_END
 }
@@ -1045,6 +1084,18 @@ extern "C" int mvd_get_plan(mvd_decon* h, int view, int* tiles, int* tile, int* 
   return MVD_OK;
 }
 
+extern "C" int mvd_get_plan_variant(mvd_decon* h, int view, int* threads, int* variant) {
+  if (!h) return fail(MVD_ERR_ARG, "NULL handle");
+  if (view < 0 || view >= h->V) return fail(MVD_ERR_ARG, "view out of range");
+  const ConvPlan& p = *h->plans[view];
+  const bool compiled = !p.generic && has_compiled_kernels(p) && p.threads_plane == kThreads;
+  if (threads) *threads = compiled && compiled_plane_threads(p) ? compiled_plane_threads(p) : p.threads_plane;
+  if (variant)
+    *variant = (compiled ? 1 : 0) | (p.ascending ? 2 : 0) |
+               (p.tensor_dft && !p.generic && tensor_dft_supported(p.az.T) ? 4 : 0);
+  return MVD_OK;
+}
+
 extern "C" int mvd_get_stream(mvd_decon* h, void** stream) {
   if (!h || !stream) return fail(MVD_ERR_ARG, "NULL argument");
   *stream = (void*)h->stream;
@@ -1092,11 +1143,8 @@ extern "C" int mvd_profile_iteration(mvd_decon* h, double* ms, int* launches) {
     launch_z(h->pt, p, sp, h->otf2[v].as<float2>(), s);
     mark(1);
     launch_inv_update(h->pt, p, sp, h->psi.as<float>(), h->w[v].as<float>(), h->lambda, &h->slot(v)->sum,
-                      &h->slot(v)->max_bits, s);
+                      &h->slot(v)->max_bits, h->archive(v), s);
     mark(3);
-    archive_stats_kernel<<<1, 1, 0, s>>>(h->slot(v), h->hist.as<double>(), h->d_iter.as<int>(), v, h->V);
-    MVD_CHECK(cudaGetLastError());
-    mark(4);
   }
   MVD_CHECK(cudaStreamSynchronize(s));
   for (size_t i = 1; i < ev.size(); ++i) {
@@ -1105,10 +1153,9 @@ extern "C" int mvd_profile_iteration(mvd_decon* h, double* ms, int* launches) {
     ms[kind[i]] += t;
     launches[kind[i]] += 1;
   }
-  launches[4] = h->V;  // the archive kernels (the last one advances the iteration counter)
   for (auto e : ev) cudaEventDestroy(e);
   ++h->iteration;
-  h->launches += 6 * h->V + h->V;
+  h->launches += 6 * h->V;
   return MVD_OK;
   MVD_API_END
 }

@@ -111,7 +111,7 @@ int next_smooth(int n, bool even) {
 }
 
 // Radices of the register DFTs (fft_device.cuh).
-static const int kRadices[] = {20, 18, 16, 15, 12, 10, 8, 6, 5, 4, 3, 2};
+static const int kRadices[] = {20, 18, 16, 15, 12, 10, 9, 8, 6, 5, 4, 3, 2};
 
 static void best_split(int n, int depth, int maxdepth, std::vector<int>& cur, std::vector<int>& best) {
   if (n == 1) {
@@ -141,14 +141,16 @@ std::vector<int> factorize(int n) {
 // ------------------------------------------------------------------------------------------
 // plan table
 // ------------------------------------------------------------------------------------------
-int PlanTable::index_of(int n) {
-  auto it = by_len_.find(n);
+int PlanTable::index_of(int n, bool ascending) {
+  const int key = ascending ? -n : n;
+  auto it = by_len_.find(key);
   if (it != by_len_.end()) return it->second;
   if (n < 1) throw std::invalid_argument("bad FFT length");
   if ((int)host_.size() >= kCapacity) throw std::runtime_error("FFT plan table full");
   FftPlan p{};
   p.n = n;
   std::vector<int> rad = factorize(n);
+  if (ascending) std::reverse(rad.begin(), rad.end());
   if ((int)rad.size() > kMaxStages) throw std::invalid_argument("too many FFT stages");
   p.nstages = (int)rad.size();
   for (size_t i = 0; i < rad.size(); ++i) p.radix[i] = rad[i];
@@ -169,7 +171,7 @@ int PlanTable::index_of(int n) {
   tw_bufs_.push_back(std::move(buf));
   const int idx = (int)host_.size();
   host_.push_back(p);
-  by_len_[n] = idx;
+  by_len_[key] = idx;
   dirty_ = true;
   return idx;
 }
@@ -390,7 +392,8 @@ std::unique_ptr<ConvPlan> make_conv_plan(PlanTable& pt, int nx, int ny, int nz, 
   p.ax = bx; p.ay = by; p.az = bz;
   const int px = bx.T / 2 + 1;
   const int pitch = row_pitch(bx.T / 2);
-  const int plx = pt.index_of(bx.T / 2), ply = pt.index_of(by.T), plz = pt.index_of(bz.T);
+  const int plx = pt.index_of(bx.T / 2, opt.ascending), ply = pt.index_of(by.T, opt.ascending),
+            plz = pt.index_of(bz.T, opt.ascending);
   const long long tile_spec = (long long)px * by.T * bz.T;
   long long off = 0;
   for (int iz = 0; iz < bz.n; ++iz)
@@ -416,6 +419,8 @@ std::unique_ptr<ConvPlan> make_conv_plan(PlanTable& pt, int nx, int ny, int nz, 
   p.otf_elems = tile_spec;
   p.smem_plane = 2 * (size_t)by.T * pitch * sizeof(float2);
   p.threads_plane = opt.threads > 0 ? opt.threads : plane_threads();
+  p.ascending = opt.ascending;
+  p.generic = opt.generic || opt.ascending;  // compiled kernels hold the descending order
   p.smem_z = 2 * (size_t)bz.T * kZPitch * sizeof(float2);
   fill_items(p);
   p.upload();
@@ -751,7 +756,7 @@ void dev_quotient(float* b, const float* img, long long n, cudaStream_t s) {
 
 __global__ void update_kernel(float* psi, const float* integral, const float* weight, float lambda, long long n,
                               double* stat_sum, unsigned* stat_max) {
-  EpiUpdate e{psi, weight, lambda, stat_sum, stat_max, 0, 0, 0.f, 0.f};
+  EpiUpdate e{psi, weight, lambda, stat_sum, stat_max, 0, 0, 0.f, 0.f, StatArchive{}};
   e.acc_init();
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
     e(i, integral[i]);

@@ -26,7 +26,7 @@ void check_cuda(cudaError_t e, const char* what);
 // 2,3,5-smooth helpers (the FFT radices are products of 2, 3 and 5)
 bool is_smooth(int n);
 int next_smooth(int n, bool even);
-std::vector<int> factorize(int n);  // radices from {20,18,16,15,12,10,8,6,5,4,3,2}, product == n
+std::vector<int> factorize(int n);  // radices from {20,18,16,15,12,10,9,8,6,5,4,3,2}, product == n
 
 // Device memory owned by RAII.  Allocated while an AllocScope is active on this thread, it
 // comes from the device's memory pool in the scope stream's order (cudaMallocAsync) and is
@@ -74,7 +74,9 @@ void keep_pool_memory(int dev);
 // Twiddle tables and FFT plans for every length used on a device.
 class PlanTable {
  public:
-  int index_of(int n);          // creates the plan if needed (host side only)
+  // creates the plan if needed (host side only); radices in the planner's descending order, or
+  // ascending (a separate plan of the same length)
+  int index_of(int n, bool ascending = false);
   const FftPlan* device();      // uploads if changed; valid until the next upload
   size_t size() const { return host_.size(); }
  private:
@@ -107,6 +109,9 @@ struct ConvPlan {
   long long otf_elems = 0;             // complex elements of one OTF (all tiles share the shape)
   size_t smem_plane = 0, smem_z = 0;
   int threads_plane = 0;               // CTA size of the plane kernels (a multiple of 32, <= kThreads)
+  bool tensor_dft = false;             // z pass with its middle DFT stage on the tensor cores (if compiled)
+  bool ascending = false;              // radices of every length in ascending order
+  bool generic = false;                // run the generic kernels even where a compiled shape exists
   DevBuf d_tiles, d_items_fwd, d_items_inv, d_items_z;
   // one tile of this shape at the origin and its work items: the OTF build's tables
   DevBuf d_otf_tile, d_otf_fwd, d_otf_z;
@@ -119,6 +124,8 @@ struct PlanOptions {
   int force_tx = 0, force_ty = 0, force_tz = 0;  // 0 = planner's choice
   int cap = 0;                                   // plane-buffer budget; 0 = plane_cap()
   int threads = 0;                               // plane CTA size; 0 = plane_threads()
+  bool ascending = false;                        // radix order of the tile's FFT lengths
+  bool generic = false;                          // generic kernels only
 };
 
 // Move a plan's tiles by (dx, dy, dz) into the frame of a larger volume `vol` whose data box
@@ -138,6 +145,18 @@ int plane_threads();
 bool use_fixed_planes();
 // L2 prefetch through tensor maps in the plane kernels (MVD_L2_PREFETCH=0 turns it off).
 bool use_l2_prefetch();
+// Whether pencils of length tz have a tensor-core z pass, and the number of its MMA waits that
+// gave up on the current device since the last call (the counter is reset; zero when none ran).
+bool tensor_dft_supported(int tz);
+int tensor_dft_failures();
+// Uploads the tensor-core z pass's DFT matrices for the current device (once; outside any stream
+// capture, since it allocates).
+void tensor_dft_prepare();
+struct ConvPlan;
+// Whether the plan's plane shape or pencil length has compiled kernels, and the CTA size of the
+// compiled plane kernels of its shape (0 if none).
+bool has_compiled_kernels(const ConvPlan& p);
+int compiled_plane_threads(const ConvPlan& p);
 // Tensor map of a float volume [nz][ny][nx] with a (w, h, 1) box (cached); false when the volume
 // does not meet the tensor copy's rules (16-byte aligned base and row stride, box <= 256).
 bool volume_box_map(const float* base, int nx, int ny, int nz, int w, int h, CUtensorMap* out);
@@ -181,7 +200,7 @@ void launch_inv_quotient(PlanTable& pt, const ConvPlan& p, const float2* spec, c
                          float* q, cudaStream_t s);
 void launch_inv_update(PlanTable& pt, const ConvPlan& p, const float2* spec, float* psi,
                        const float* weight, float lambda, double* stat_sum, unsigned* stat_max,
-                       cudaStream_t s);
+                       const StatArchive& archive, cudaStream_t s);
 
 // Kernel launches issued by this library (all devices), for launch accounting.
 long long launch_count();

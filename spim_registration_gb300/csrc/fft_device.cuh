@@ -31,7 +31,7 @@ constexpr int kMaxStages = 6;
 struct FftPlan {
   int n;                    // transform length
   int nstages;              // number of radix stages
-  int radix[kMaxStages];    // radices (each in {2,3,4,5,6,8,10,12,15,16,18,20}), product == n
+  int radix[kMaxStages];    // radices (each in {2,3,4,5,6,8,9,10,12,15,16,18,20}), product == n
   const float2* tw;         // exp(-2 pi i k / n), k in [0, n)
   const float2* tw_r2c;     // for the real-input length 2n: exp(-2 pi i k / (2n)), k in [0, n]
 };
@@ -314,6 +314,7 @@ __device__ __forceinline__ void stage(int R, int N, int Ns, int count, const flo
     case 5: stage_r<5, INV, JFAST>(N, Ns, count, tw, ld, st); break;
     case 6: stage_r<6, INV, JFAST>(N, Ns, count, tw, ld, st); break;
     case 8: stage_r<8, INV, JFAST>(N, Ns, count, tw, ld, st); break;
+    case 9: stage_r<9, INV, JFAST>(N, Ns, count, tw, ld, st); break;
     case 10: stage_r<10, INV, JFAST>(N, Ns, count, tw, ld, st); break;
     case 12: stage_r<12, INV, JFAST>(N, Ns, count, tw, ld, st); break;
     case 15: stage_r<15, INV, JFAST>(N, Ns, count, tw, ld, st); break;
@@ -358,6 +359,7 @@ __device__ __forceinline__ void zmid(int R, int N, int count, const float2* __re
     case 5: zmid_r<5>(N, count, tw, ld, mul, st); break;
     case 6: zmid_r<6>(N, count, tw, ld, mul, st); break;
     case 8: zmid_r<8>(N, count, tw, ld, mul, st); break;
+    case 9: zmid_r<9>(N, count, tw, ld, mul, st); break;
     case 10: zmid_r<10>(N, count, tw, ld, mul, st); break;
     case 12: zmid_r<12>(N, count, tw, ld, mul, st); break;
     case 15: zmid_r<15>(N, count, tw, ld, mul, st); break;

@@ -14,13 +14,13 @@
 namespace mvd {
 
 // The planner's factorisation (engine.cu factorize): fewest stages, then the largest smallest
-// radix, radices non-increasing, from {20, 18, 16, 15, 12, 10, 8, 6, 5, 4, 3, 2}.
+// radix, radices non-increasing, from {20, 18, 16, 15, 12, 10, 9, 8, 6, 5, 4, 3, 2}.
 struct SplitC {
   int s = 0;
   int r[kMaxStages] = {0, 0, 0, 0, 0, 0};
 };
 
-constexpr int kRadixList[12] = {20, 18, 16, 15, 12, 10, 8, 6, 5, 4, 3, 2};
+constexpr int kRadixList[13] = {20, 18, 16, 15, 12, 10, 9, 8, 6, 5, 4, 3, 2};
 
 __host__ __device__ constexpr int split_min(const SplitC& c) {
   int m = 1 << 30;
@@ -37,7 +37,7 @@ __host__ __device__ constexpr void split_search(int n, int depth, int maxdepth, 
     return;
   }
   if (depth == maxdepth) return;
-  for (int i = 0; i < 12; ++i) {
+  for (int i = 0; i < 13; ++i) {
     const int r = kRadixList[i];
     if (n % r) continue;
     if (cur.s && r > cur.r[cur.s - 1]) continue;
@@ -127,7 +127,8 @@ __host__ __device__ constexpr int ns_before(int s) {
 
 // Stages s .. S-1 of a length-N transform whose result stays in shared memory (the generic
 // run_transform_smem): stage 0 loads with ld0, every stage writes the other buffer.
-template <int N, int s, bool INV, bool ROWS, bool ROW_G0, int ES, int BS, int T, class LD0>
+// SKEW: the first row stage (ROW_G0) writes the skewed layout i + i/16 and the second reads it.
+template <int N, int s, bool INV, bool ROWS, bool ROW_G0, int ES, int BS, int T, bool SKEW = true, class LD0>
 __device__ __forceinline__ void smem_stages(int count, const float2* __restrict__ tw, const LD0& ld0, float2*& cur,
                                             float2*& oth) {
   constexpr SplitC sp = split_of(N);
@@ -135,19 +136,29 @@ __device__ __forceinline__ void smem_stages(int count, const float2* __restrict_
     constexpr int R = sp.r[s];
     constexpr int NS = ns_before<N>(s);
     if constexpr (s == 0) {
-      constexpr bool skew_out = ROWS && ROW_G0 && sp.s > 1;
+      constexpr bool skew_out = SKEW && ROWS && ROW_G0 && sp.s > 1;
       stage_c<R, N, NS, INV, ROWS && ROW_G0, T>(count, tw, ld0, SmemC<ES, BS, skew_out>{oth});
     } else {
-      constexpr bool skew_in = ROWS && ROW_G0 && s == 1;
+      constexpr bool skew_in = SKEW && ROWS && ROW_G0 && s == 1;
       stage_c<R, N, NS, INV, false, T>(count, tw, SmemC<ES, BS, skew_in>{cur}, SmemC<ES, BS, false>{oth});
     }
     __syncthreads();
     float2* t = cur;
     cur = oth;
     oth = t;
-    smem_stages<N, s + 1, INV, ROWS, ROW_G0, ES, BS, T>(count, tw, ld0, cur, oth);
+    smem_stages<N, s + 1, INV, ROWS, ROW_G0, ES, BS, T, SKEW>(count, tw, ld0, cur, oth);
   }
 }
+
+// Shared-memory row layout of a compiled plane shape, chosen per shape with a wavefront model of
+// the forward pass's shared accesses (float2 accesses, 16 bank pairs per half warp): whether the
+// first row stage, which maps butterflies j-fastest, writes the skewed layout i + i/16, and the
+// row pitch (odd, so that batch-fastest row stages are conflict-free).  The skew suits 128-wide
+// tiles (radix 8 x 8); for 100, 160 and 192-wide tiles the plain layout gives 7-46% fewer
+// wavefronts (160x160: 4986 against 9280 per slice), because their first-stage stride (10 or
+// 12) already spreads a row's positions over the banks.
+__host__ __device__ constexpr bool fixed_skew(int TX) { return TX == 128; }
+__host__ __device__ constexpr int fixed_pitch(int TX) { return fixed_skew(TX) ? row_pitch(TX / 2) : ((TX / 2 + 1) | 1); }
 
 // All stages with the last storing through stl (the generic run_transform_to).
 template <int N, int s, bool INV, bool ROWS, int ES, int BS, int T, class LD0, class STL>
@@ -174,11 +185,16 @@ __device__ __forceinline__ void to_stages(int count, const float2* __restrict__ 
   }
 }
 
-// CTAs per SM the register allocation of a compiled-shape plane kernel is sized for: planes of
-// up to ~100 KB per buffer run 512-thread CTAs, two per SM (at most 64 registers a thread);
-// larger planes leave room for one CTA per SM, which then runs 1024 threads (also 64 registers)
-// so that twice as many warps hide the latency of the gathers and the shared-memory exchanges.
-__host__ __device__ constexpr int fixed_ctas_per_sm(int threads) { return threads >= 1024 ? 1 : 2; }
+// CTAs per SM a compiled-shape plane kernel is sized for: two when two CTAs' buffers (two
+// planes of TY rows at the row pitch each) fit the SM's shared memory, else one.  The register
+// allocation follows (T threads x CTAs within the 64K registers of an SM).  Planes of up to
+// ~100 KB per buffer run 512-thread CTAs, two per SM; larger planes run one 1024-thread CTA per
+// SM, so that twice as many warps hide the latency of the gathers and the exchanges (on the
+// 512x512x256 workload 1024 threads measured 23.5 G voxel-updates/s, 768 threads 23.0, 512
+// threads 21.3).
+__host__ __device__ constexpr int fixed_ctas_per_sm(int TX, int TY) {
+  return 2 * (2 * TY * row_pitch(TX / 2) * 8) <= 227 * 1024 ? 2 : 1;
+}
 
 // Forward plane pass: the generic kernel's structure (the first row stage gathers straight from
 // the volume, j-fastest) with the shape fixed.  Staging the slice in shared memory first, for
@@ -188,10 +204,10 @@ __host__ __device__ constexpr int fixed_ctas_per_sm(int threads) { return thread
 // TY, 1) box; each CTA prefetches into L2 the slice of the CTA `ahead` launches later (one
 // resident wave on), so the next wave's gathers find their rows there.
 template <class Gather, int TX, int TY, int T>
-__global__ void __launch_bounds__(T, fixed_ctas_per_sm(T))
+__global__ void __launch_bounds__(T, fixed_ctas_per_sm(TX, TY))
 plane_fwd_fixed(const TileDesc* __restrict__ tiles, const int2* __restrict__ items, const FftPlan* __restrict__ plans,
                 float2* __restrict__ spec, Gather gather, const __grid_constant__ EpiBoxes src, int ahead) {
-  constexpr int M = TX / 2, PX = M + 1, PITCH = row_pitch(M);
+  constexpr int M = TX / 2, PX = M + 1, PITCH = fixed_pitch(TX);
   extern __shared__ float2 sm[];
   const int2 it = items[blockIdx.x];
   const TileDesc t = tiles[it.x];
@@ -206,7 +222,7 @@ plane_fwd_fixed(const TileDesc* __restrict__ tiles, const int2* __restrict__ ite
   float2* oth = sm + TY * PITCH;
   RowGather<Gather, false> ld0{gather, t.ox, t.oy, t.oz + z, 0, 0, 0, 0, true};
   const FftPlan* pxp = plans + t.plan_x;
-  smem_stages<M, 0, false, true, true, 1, PITCH, T>(TY, pxp->tw, ld0, cur, oth);
+  smem_stages<M, 0, false, true, true, 1, PITCH, T, fixed_skew(TX)>(TY, pxp->tw, ld0, cur, oth);
   SpecSliceStore st{spec + t.spec_off + (long long)z * TY * PX, PX};
   to_stages<TY, 0, false, false, PITCH, 1, T>(PX, plans[t.plan_y].tw, R2CColumnLoad{cur, PITCH, M, pxp->tw_r2c}, st,
                                              cur, oth);
@@ -216,10 +232,10 @@ plane_fwd_fixed(const TileDesc* __restrict__ tiles, const int2* __restrict__ ite
 // effective rows stays in shared memory (batch-fastest stages), and the epilogue then walks the
 // effective region by whole warps per row: psi / weight / img accesses are fully coalesced.
 template <class Epi, int TX, int TY, int T>
-__global__ void __launch_bounds__(T, fixed_ctas_per_sm(T))
+__global__ void __launch_bounds__(T, fixed_ctas_per_sm(TX, TY))
 plane_inv_fixed(const TileDesc* __restrict__ tiles, const int2* __restrict__ items, const FftPlan* __restrict__ plans,
                 const float2* __restrict__ spec, Epi epi, const __grid_constant__ EpiBoxes boxes) {
-  constexpr int M = TX / 2, PX = M + 1, PITCH = row_pitch(M);
+  constexpr int M = TX / 2, PX = M + 1, PITCH = fixed_pitch(TX);
   extern __shared__ float2 sm[];
   const int2 it = items[blockIdx.x];
   const TileDesc t = tiles[it.x];
@@ -372,12 +388,13 @@ __host__ __device__ constexpr int zpass_fixed_occ(int TZ) {
 
 // Tile shapes (x length, y length, CTA size) with compiled kernels.  They replace the default
 // 384-thread generic kernels: a plan whose CTA size is the default runs them at their own size.
-// 100x100 and 128x100: the 256x256x192 workload's planes (two CTAs per SM); 160x160 and 192x96:
-// the 512x512x256 workload's (one CTA per SM).
+// 100x100 and 128x100: the 256x256x192 workload's planes (two CTAs per SM); 160x160, 192x96 and
+// 192x135: the 512x512x256 workload's (one CTA per SM).
 #define MVD_FIXED_PLANE_SHAPES(X) \
   X(100, 100, 512)                \
   X(128, 100, 512)                \
   X(160, 160, 1024)               \
-  X(192, 96, 1024)
+  X(192, 96, 1024)                \
+  X(192, 135, 1024)
 
 }  // namespace mvd

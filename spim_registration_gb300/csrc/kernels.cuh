@@ -204,6 +204,18 @@ struct EpiQuotient {
   __device__ __forceinline__ void finish() {}
 };
 
+// Where the update pass files a view's statistics once its last CTA is done: the history ring
+// hist[(iteration % slots) * nviews + view] = (sum, max), after which the running sums are
+// cleared for the view's next update and, after the last view, the iteration counter advances.
+// `ticket` counts finished CTAs (the last one archives and resets it).  hist == nullptr: no
+// archive (the sums are left for the caller).
+struct StatArchive {
+  double* hist;
+  int* iter;
+  unsigned* ticket;
+  int view, nviews, slots;
+};
+
 // MVDeconvolution.computeFinalValues / computeNextValue / tikhonov (:603-726).  The reference
 // evaluates tikhonov in double and rounds to float; here the algebraically equal form
 // 2v / (sqrt(1 + 2 lambda v) + 1) is evaluated in float (no cancellation, within a few ulp).
@@ -217,6 +229,7 @@ struct EpiUpdate {
   int nx, ny;
   float acc_sum;
   float acc_max;
+  StatArchive archive;
   int inputs(const float** p) const {
     p[0] = psi;
     p[1] = weight;
@@ -294,6 +307,23 @@ struct EpiUpdate {
       if (lane == 0) {
         atomicAdd(stat_sum, sum);
         atomicMax(stat_max, __float_as_uint(mx));
+        if (archive.hist) {
+          // the CTA that finishes last files the view's totals (the threadfence-reduction pattern:
+          // every CTA's atomics are visible before its ticket)
+          __threadfence();
+          if (atomicAdd(archive.ticket, 1u) == gridDim.x - 1) {
+            __threadfence();
+            const double total = atomicAdd(stat_sum, 0.0);
+            const unsigned mbits = atomicMax(stat_max, 0u);
+            const int it = *archive.iter % archive.slots;
+            archive.hist[(it * archive.nviews + archive.view) * 2 + 0] = total;
+            archive.hist[(it * archive.nviews + archive.view) * 2 + 1] = (double)__uint_as_float(mbits);
+            *stat_sum = 0.0;
+            *stat_max = 0u;
+            *archive.ticket = 0u;
+            if (archive.view == archive.nviews - 1) *archive.iter += 1;
+          }
+        }
       }
     }
   }

@@ -39,7 +39,7 @@ static bool launch_fwd_fixed(int tx, int ty, int threads, PlanTable& pt, const T
                 volume_box_map(g.v.data, g.v.nx, g.v.ny, g.v.nz, prefetch_box_width(TX), TY, &src.map[0]); \
     auto k = plane_fwd_fixed<Gather, TX, TY, T>;                                                        \
     set_smem(k, smem);                                                                                  \
-    k<<<nitems, T, smem, s>>>(tiles, items, pt.device(), spec, g, src, resident_ctas(fixed_ctas_per_sm(T))); \
+    k<<<nitems, T, smem, s>>>(tiles, items, pt.device(), spec, g, src, resident_ctas(fixed_ctas_per_sm(TX, TY))); \
     return true;                                                                                        \
   }
   MVD_FIXED_PLANE_SHAPES(MVD_FWD_CASE)
@@ -47,12 +47,30 @@ static bool launch_fwd_fixed(int tx, int ty, int threads, PlanTable& pt, const T
   return false;
 }
 
+int compiled_plane_threads(const ConvPlan& p) {
+#define MVD_SHAPE_T(SX, SY, ST) \
+  if (p.ax.T == SX && p.ay.T == SY) return ST;
+  MVD_FIXED_PLANE_SHAPES(MVD_SHAPE_T)
+#undef MVD_SHAPE_T
+  return 0;
+}
+
+bool has_compiled_kernels(const ConvPlan& p) {
+  if (compiled_plane_threads(p)) return true;
+#define MVD_Z_LEN(SZ) \
+  if (p.az.T == SZ) return true;
+  MVD_FIXED_Z_LENGTHS(MVD_Z_LEN)
+#undef MVD_Z_LEN
+  return false;
+}
+
 template <class Gather, bool MASK = false>
 static void launch_fwd_impl(PlanTable& pt, const TileDesc* tiles, const int2* items, int nitems, size_t smem,
-                            int threads, int tx, int ty, float2* spec, Gather g, cudaStream_t s) {
+                            int threads, int tx, int ty, float2* spec, Gather g, cudaStream_t s,
+                            bool generic = false) {
   if (nitems == 0) return;
-  if (MASK || !launch_fwd_fixed(tx, ty, threads > 0 ? threads : kThreads, pt, tiles, items, nitems, smem, spec, g,
-                                s)) {
+  if (MASK || generic ||
+      !launch_fwd_fixed(tx, ty, threads > 0 ? threads : kThreads, pt, tiles, items, nitems, smem, spec, g, s)) {
     EpiBoxes src;
     std::memset(&src, 0, sizeof(src));
     src.count = !MASK && use_l2_prefetch() &&
@@ -70,7 +88,7 @@ static void launch_fwd_impl(PlanTable& pt, const TileDesc* tiles, const int2* it
 void launch_fwd_mirror(PlanTable& pt, const ConvPlan& p, const float* vol, float2* spec, cudaStream_t s) {
   GatherMirror g{{vol, p.vol[0], p.vol[1], p.vol[2]}};
   launch_fwd_impl(pt, p.d_tiles.as<TileDesc>(), p.d_items_fwd.as<int2>(), (int)p.items_fwd.size(), p.smem_plane,
-                  p.threads_plane, p.ax.T, p.ay.T, spec, g, s);
+                  p.threads_plane, p.ax.T, p.ay.T, spec, g, s, p.generic);
 }
 
 void launch_fwd_value(PlanTable& pt, const ConvPlan& p, const float* vol, float value, float2* spec,
@@ -78,13 +96,13 @@ void launch_fwd_value(PlanTable& pt, const ConvPlan& p, const float* vol, float 
   GatherValue g = GatherValue::box(vol, p.vol[0], p.vol[1], p.vol[2], value, p.box_lo[0], p.box_lo[1], p.box_lo[2],
                                    p.box_hi[0], p.box_hi[1], p.box_hi[2]);
   launch_fwd_impl(pt, p.d_tiles.as<TileDesc>(), p.d_items_fwd.as<int2>(), (int)p.items_fwd.size(), p.smem_plane,
-                  p.threads_plane, p.ax.T, p.ay.T, spec, g, s);
+                  p.threads_plane, p.ax.T, p.ay.T, spec, g, s, p.generic);
 }
 
 void launch_fwd_value_items(PlanTable& pt, const ConvPlan& p, const TileDesc* tiles, const int2* items, int nitems,
                             const float* vol, int vx, int vy, int vz, float value, float2* spec, cudaStream_t s) {
   GatherValue g = GatherValue::full(vol, vx, vy, vz, value);
-  launch_fwd_impl(pt, tiles, items, nitems, p.smem_plane, p.threads_plane, p.ax.T, p.ay.T, spec, g, s);
+  launch_fwd_impl(pt, tiles, items, nitems, p.smem_plane, p.threads_plane, p.ax.T, p.ay.T, spec, g, s, p.generic);
 }
 
 void launch_fwd_masked(PlanTable& pt, const ConvPlan& p, const float* vol, float2* spec, cudaStream_t s) {

@@ -27,7 +27,7 @@ template <class Epi>
 static bool launch_inv_fixed(PlanTable& pt, const ConvPlan& p, const TileDesc* tiles, const int2* items, int nitems,
                              const float2* spec, Epi e, cudaStream_t s) {
   const int threads = p.threads_plane > 0 ? p.threads_plane : kThreads;
-  if (threads != kThreads || !use_fixed_planes()) return false;
+  if (threads != kThreads || p.generic || !use_fixed_planes()) return false;
   const int tx = p.ax.T, ty = p.ay.T;
   const EpiBoxes boxes = epilogue_boxes(p, e);
 #define MVD_INV_CASE(TX, TY, T)                                                        \
@@ -69,8 +69,9 @@ void launch_inv_quotient(PlanTable& pt, const ConvPlan& p, const float2* spec, c
 }
 
 void launch_inv_update(PlanTable& pt, const ConvPlan& p, const float2* spec, float* psi, const float* weight,
-                       float lambda, double* stat_sum, unsigned* stat_max, cudaStream_t s) {
-  EpiUpdate e{psi, weight, lambda, stat_sum, stat_max, p.vol[0], p.vol[1], 0.f, 0.f};
+                       float lambda, double* stat_sum, unsigned* stat_max, const StatArchive& archive,
+                       cudaStream_t s) {
+  EpiUpdate e{psi, weight, lambda, stat_sum, stat_max, p.vol[0], p.vol[1], 0.f, 0.f, archive};
   launch_inv_impl(pt, p, spec, e, s);
 }
 

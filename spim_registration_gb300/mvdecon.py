@@ -35,6 +35,7 @@ class PSFTYPE(enum.IntEnum):
 FLAG_PLAIN = 1
 FLAG_NO_GRAPH = 2
 FLAG_AUTOTUNE = 4
+FLAG_TENSOR_DFT = 8  # middle 16-point DFTs of the 320 / 288 z passes on the tensor cores
 
 
 def FLAG_REF_SUM_THREADS(threads: int) -> int:
@@ -296,7 +297,12 @@ class Deconvolution:
         t, s, e = (ctypes.c_int * 3)(), (ctypes.c_int * 3)(), (ctypes.c_int * 3)()
         pv = ctypes.c_longlong()
         native.check(self.lib.mvd_get_plan(self.h, view, t, s, e, ctypes.byref(pv)))
-        return dict(tiles=tuple(t), tile=tuple(s), effective=tuple(e), padded_voxels=pv.value)
+        th, var = ctypes.c_int(), ctypes.c_int()
+        native.check(self.lib.mvd_get_plan_variant(self.h, view, ctypes.byref(th), ctypes.byref(var)))
+        return dict(tiles=tuple(t), tile=tuple(s), effective=tuple(e), padded_voxels=pv.value,
+                    threads=th.value, kernels="compiled" if var.value & 1 else "generic",
+                    radix_order="ascending" if var.value & 2 else "descending",
+                    tensor_dft=bool(var.value & 4))
 
 
 class MVDeconvolution:

@@ -67,6 +67,7 @@ SIGNATURES = {
     "mvd_get_stats": (ctypes.c_int, [_H, ctypes.c_int, ctypes.c_int, _D, _D]),
     "mvd_get_iteration": (ctypes.c_int, [_H, _I]),
     "mvd_get_plan": (ctypes.c_int, [_H, ctypes.c_int, _I, _I, _I, _LL]),
+    "mvd_get_plan_variant": (ctypes.c_int, [_H, ctypes.c_int, _I, _I]),
     "mvd_get_stream": (ctypes.c_int, [_H, ctypes.POINTER(ctypes.c_void_p)]),
     "mvd_get_launch_count": (ctypes.c_int, [_H, _LL]),
     "mvd_profile_iteration": (ctypes.c_int, [_H, _D, _I]),

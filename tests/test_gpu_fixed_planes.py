@@ -24,6 +24,8 @@ SCRIPT = textwrap.dedent("""
     from spim_registration_gb300 import synthetic as S
     if sys.argv[2] == "large":  # the 512x512x256 workload's PSFs: 160x160 / 192x96 planes, 320 / 288 pencils
         p = S.make_problem(4, shape_xyz=(260, 260, 256), psf_size_xyz=(31, 31, 61), n_blobs=60, iterations=1)
+    elif sys.argv[2] == "large135":  # 192x135 planes (radices 15 x 9 along y)
+        p = S.make_problem(4, shape_xyz=(248, 210, 256), psf_size_xyz=(31, 31, 61), n_blobs=60, iterations=1)
     elif sys.argv[2] == "full":
         p = S.make_problem(2, shape_xyz=(172, 172, 192), psf_size_xyz=(15, 15, 41), n_blobs=40, iterations=2)
     else:  # data boxes smaller than the volume in x, y and z, still planned with 100/128-wide tiles
@@ -57,13 +59,14 @@ def test_fixed_shape_kernels_equal_the_generic_kernels(tmp_path):
     np.testing.assert_array_equal(np.load(a), np.load(b))
 
 
-@pytest.mark.parametrize("cap,plane", [(14336, "160x160x"), (10240, "192x96x")])
-def test_large_psf_shapes_equal_the_generic_kernels(tmp_path, cap, plane):
-    """1024-thread compiled planes and the 320 / 288 compiled pencils (radices 20 and 18) of the
-    31x31x61-PSF workload against the generic kernels, bit for bit."""
+@pytest.mark.parametrize("cap,plane,case", [(14336, "160x160x", "large"), (10240, "192x96x", "large"),
+                                            (14336, "192x135x", "large135")])
+def test_large_psf_shapes_equal_the_generic_kernels(tmp_path, cap, plane, case):
+    """1024-thread compiled planes (plain row layout) and the 320 / 288 compiled pencils (radices
+    20 and 18) of the 31x31x61-PSF workload against the generic kernels, bit for bit."""
     a, b = str(tmp_path / "fixed.npy"), str(tmp_path / "generic.npy")
-    shapes = _run(a, True, "large", cap)
-    assert _run(b, False, "large", cap) == shapes
+    shapes = _run(a, True, case, cap)
+    assert _run(b, False, case, cap) == shapes
     assert any(t.startswith(plane) for t in shapes), shapes
     assert any(t.endswith("x320") for t in shapes) and (cap == 14336 or any(t.endswith("x288") for t in shapes))
     np.testing.assert_array_equal(np.load(a), np.load(b))
