@@ -71,8 +71,11 @@ def parse():
     ap.add_argument("--no-tensor-dft", action="store_true", help="skip the tensor-core DFT stage object")
     ap.add_argument("--tensor-dft", action="store_true",
                     help="time the handle with the tensor-core middle DFT stages as the line's value")
-    ap.add_argument("--only", choices=["inputs", "separable"],
-                    help="measure only the input preparation or the separable convolution at the workload's size")
+    ap.add_argument("--only", choices=["inputs", "separable", "stage"],
+                    help="measure only the input preparation or the separable convolution at the workload's size; "
+                         "'stage': run --warmup + --steps iterations of the workload (untimed, for profilers)")
+    ap.add_argument("--volume", default=None,
+                    help="x,y,z size of the workload's synthetic volume (default: the workload's own)")
     return ap.parse_args()
 
 
@@ -137,11 +140,14 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def make_problem(workload):
+def make_problem(workload, volume=None):
     """The workload's seeded inputs; MVD_PROBLEM_CACHE=<dir> keeps them between runs."""
     from spim_registration_gb300 import synthetic as S
 
     cfg, shape, psf, _ = WORKLOADS[workload]
+    if volume is not None:
+        shape = tuple(int(v) for v in volume.split(","))
+        workload = f"{workload}_at_{shape[0]}x{shape[1]}x{shape[2]}"
     cache = os.environ.get("MVD_PROBLEM_CACHE")
     path = os.path.join(cache, workload + ".npz") if cache else None
     if path and os.path.exists(path):
@@ -202,6 +208,19 @@ def max_over_ranks(ms: float, world: int) -> float:
 def replica_value(units_per_rank: float, ms_max: float, world: int) -> float:
     """Whole-job throughput of `world` independent replicas: all ranks' units / the max time."""
     return units_per_rank * world / (ms_max / 1e3)
+
+
+def run_stage(prob, local, args):
+    """Iterations of the workload for a profiler: the handle with the bench's flags, --warmup +
+    --steps iterations, nothing timed; prints the plans."""
+    from spim_registration_gb300 import FLAG_AUTOTUNE, FLAG_TENSOR_DFT, Deconvolution
+
+    flags = (0 if args.no_autotune else FLAG_AUTOTUNE) | (FLAG_TENSOR_DFT if args.tensor_dft else 0)
+    with Deconvolution(prob.views, prob.weights, prob.psfs, prob.psftype, prob.lam, local, flags) as dec:
+        dec.run(args.warmup + args.steps)
+        dec.synchronize()
+        return {"workload": args.workload, "volume_xyz": list(prob.dims_xyz), "iterations": args.warmup + args.steps,
+                "plans": [dec.plan(v) for v in range(len(prob.views))]}
 
 
 def time_iterations(dec, stream, steps, world=1, clocks=None):
@@ -288,7 +307,9 @@ def run_ours(args, rank, world, local):
     hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
     peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
 
-    prob = make_problem(args.workload)
+    prob = make_problem(args.workload, args.volume)
+    if args.only == "stage":
+        return run_stage(prob, local, args)
     if args.only:
         part = {"inputs": ("input_preparation", run_inputs), "separable": ("separable_convolution", run_separable)}
         key, fn = part[args.only]

@@ -739,8 +739,13 @@ std::unique_ptr<ConvPlan> plan_view(mvd_decon* h, int v, const int lo[3], const 
       int threads;
       bool generic;
     };
-    std::vector<Variant> variants{{kThreads, false}, {256, true}};
-    if (has_compiled_kernels(*p)) variants.push_back({kThreads, true});
+    // the tensor-core z pass runs with the compiled kernels only: with it asked for, they are
+    // the one variant timed (the generic and ascending-radix candidates would drop it)
+    std::vector<Variant> variants{{kThreads, false}};
+    if (!tensor_dft) {
+      variants.push_back({256, true});
+      if (has_compiled_kernels(*p)) variants.push_back({kThreads, true});
+    }
     float ms = 1e30f;
     Variant bv = variants[0];
     for (const Variant& var : variants) {
@@ -754,11 +759,13 @@ std::unique_ptr<ConvPlan> plan_view(mvd_decon* h, int v, const int lo[3], const 
     }
     p->threads_plane = bv.threads;
     p->generic = bv.generic;
-    auto asc = make(cap, true);
-    const float t_asc = time_stage(*asc, otf, spec);
-    if (t_asc < ms) {
-      ms = t_asc;
-      p = std::move(asc);
+    if (!tensor_dft) {
+      auto asc = make(cap, true);
+      const float t_asc = time_stage(*asc, otf, spec);
+      if (t_asc < ms) {
+        ms = t_asc;
+        p = std::move(asc);
+      }
     }
     if (ms < best_ms) {
       best_ms = ms;
