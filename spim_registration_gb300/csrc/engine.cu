@@ -212,17 +212,24 @@ static std::vector<AxisTiles> axis_options(int size, int k, bool even, int tmax)
   return out;
 }
 
+// Work items of the three passes.  Plane passes: tile by tile, slice by slice.  z pass: pencil
+// chunk by chunk, every tile's chunk in turn -- all tiles of a plan share one kernel spectrum
+// (the OTF), so CTAs launched together read the same OTF chunk, which then stays in L2 (tile by
+// tile, a view's OTF of up to 33 MB is read once per tile and falls out of L2 between tiles).
 static void fill_items(ConvPlan& p) {
   p.items_fwd.clear();
   p.items_inv.clear();
   p.items_z.clear();
+  int plane_max = 0;
   for (int i = 0; i < (int)p.tiles.size(); ++i) {
     const TileDesc& t = p.tiles[i];
     for (int z = 0; z < t.tz; ++z) p.items_fwd.push_back(make_int2(i, z));
     for (int z = t.hz; z < t.hz + t.ez; ++z) p.items_inv.push_back(make_int2(i, z));
-    const int plane = t.ty * t.px;
-    for (int p0 = 0; p0 < plane; p0 += kZChunk) p.items_z.push_back(make_int2(i, p0));
+    plane_max = std::max(plane_max, t.ty * t.px);
   }
+  for (int p0 = 0; p0 < plane_max; p0 += kZChunk)
+    for (int i = 0; i < (int)p.tiles.size(); ++i)
+      if (p0 < p.tiles[i].ty * p.tiles[i].px) p.items_z.push_back(make_int2(i, p0));
 }
 
 void ConvPlan::upload() {
