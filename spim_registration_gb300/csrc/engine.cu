@@ -212,10 +212,14 @@ static std::vector<AxisTiles> axis_options(int size, int k, bool even, int tmax)
   return out;
 }
 
-// Work items of the three passes.  Plane passes: tile by tile, slice by slice.  z pass: pencil
-// chunk by chunk, every tile's chunk in turn -- all tiles of a plan share one kernel spectrum
-// (the OTF), so CTAs launched together read the same OTF chunk, which then stays in L2 (tile by
-// tile, a view's OTF of up to 33 MB is read once per tile and falls out of L2 between tiles).
+// Work items of the three passes.  Plane passes: tile by tile, slice by slice.  z pass: blocks
+// of kZBlock consecutive pencil chunks, each block swept over every tile before the next.  All
+// tiles of a plan share one kernel spectrum (the OTF), so a block's OTF chunks stay in L2 while
+// every tile reads them, and each tile's reads stay contiguous over the block.  (Tile by tile,
+// a view's OTF of up to 33 MB was re-read from DRAM for every tile; chunk by chunk across tiles,
+// consecutive CTAs read 16 tiles' scattered chunks and the z pass got slower: 3.62 ms against
+// 3.43 ms per iteration on the 512x512x256 workload.)
+constexpr int kZBlock = 32;
 static void fill_items(ConvPlan& p) {
   p.items_fwd.clear();
   p.items_inv.clear();
@@ -227,9 +231,12 @@ static void fill_items(ConvPlan& p) {
     for (int z = t.hz; z < t.hz + t.ez; ++z) p.items_inv.push_back(make_int2(i, z));
     plane_max = std::max(plane_max, t.ty * t.px);
   }
-  for (int p0 = 0; p0 < plane_max; p0 += kZChunk)
-    for (int i = 0; i < (int)p.tiles.size(); ++i)
-      if (p0 < p.tiles[i].ty * p.tiles[i].px) p.items_z.push_back(make_int2(i, p0));
+  for (int b0 = 0; b0 < plane_max; b0 += kZBlock * kZChunk)
+    for (int i = 0; i < (int)p.tiles.size(); ++i) {
+      const int plane = p.tiles[i].ty * p.tiles[i].px;
+      for (int p0 = b0; p0 < std::min(plane, b0 + kZBlock * kZChunk); p0 += kZChunk)
+        p.items_z.push_back(make_int2(i, p0));
+    }
 }
 
 void ConvPlan::upload() {

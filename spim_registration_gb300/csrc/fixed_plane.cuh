@@ -218,6 +218,11 @@ plane_fwd_fixed(const TileDesc* __restrict__ tiles, const int2* __restrict__ ite
     int zsrc;
     if (gather.slice_source(t2.oz + it2.y, zsrc)) prefetch_box_l2(&src.map[0], t2.ox & ~3, t2.oy, zsrc);
   }
+  float cval;
+  if (gather.constant_slice(t.oz + z, cval)) {  // a slice of the extension value only
+    constant_spectrum_slice(spec + t.spec_off + (long long)z * TY * PX, TX, TY, PX, cval);
+    return;
+  }
   float2* cur = sm;
   float2* oth = sm + TY * PITCH;
   RowGather<Gather, false> ld0{gather, t.ox, t.oy, t.oz + z, 0, 0, 0, 0, true};

@@ -113,6 +113,8 @@ struct GatherMirror {  // psi extended mirror-single (MVDeconFFTThreads.java:44,
   __device__ __forceinline__ void region(int& x0, int& x1, int& y0, int& y1) const {
     x0 = 0; x1 = v.nx; y0 = 0; y1 = v.ny;
   }
+  // whether every value of slice gz is one constant (never: the mirror reads the volume)
+  __device__ __forceinline__ bool constant_slice(int, float&) const { return false; }
 };
 
 struct GatherValue {  // quotient extended with a constant (value 1: MVDeconFFTThreads.java:63,103)
@@ -152,7 +154,21 @@ struct GatherValue {  // quotient extended with a constant (value 1: MVDeconFFTT
   __device__ __forceinline__ void region(int& x0, int& x1, int& y0, int& y1) const {
     x0 = lo[0]; x1 = hi[0]; y0 = lo[1]; y1 = hi[1];
   }
+  // whether every value of slice gz is one constant: a slice outside the data box is `value`
+  __device__ __forceinline__ bool constant_slice(int gz, float& c) const {
+    c = value;
+    return gz < lo[2] || gz >= hi[2];
+  }
 };
+
+// The half-spectrum slice [y][kx] of a constant slice c of tx x ty reals: the DC term c tx ty,
+// zero elsewhere (the forward transform is unnormalised).  The second convolution's input is
+// extended with the value 1 outside the view's data box, so the slices of a tile's z halo that
+// lie outside the box take this path instead of a gather and two transforms.
+__device__ __forceinline__ void constant_spectrum_slice(float2* p, int tx, int ty, int px, float c) {
+  const int n = ty * px;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) p[i] = make_float2(i == 0 ? c * (float)tx * (float)ty : 0.f, 0.f);
+}
 
 // ------------------------------------------------------------------------------------------
 // epilogues of the inverse plane pass.  apply<K>(g0, off, val, ok) handles K voxels of one row
@@ -623,6 +639,11 @@ plane_fwd_kernel(const TileDesc* __restrict__ tiles, const int2* __restrict__ it
     const TileDesc t2 = tiles[it2.x];
     int zsrc;
     if (gather.slice_source(t2.oz + it2.y, zsrc)) prefetch_box_l2(&src.map[0], t2.ox & ~3, t2.oy, zsrc);
+  }
+  float cval;
+  if (!MASK && gather.constant_slice(t.oz + z, cval)) {
+    constant_spectrum_slice(spec + t.spec_off + (long long)z * t.ty * t.px, t.tx, t.ty, t.px, cval);
+    return;
   }
   const int M = t.tx / 2;
   float2* cur = sm;
