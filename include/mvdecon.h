@@ -67,7 +67,9 @@ enum {
   MVD_FLAG_PLAIN = 1,    /* reference structure: one block per launch sequence, separate
                             quotient / update kernels, no graph (the plain FP32 GPU form) */
   MVD_FLAG_NO_GRAPH = 2, /* batched, fused passes but launched eagerly (no CUDA graph) */
-  MVD_FLAG_AUTOTUNE = 4, /* time candidate tile plans per view at creation and keep the fastest */
+  MVD_FLAG_AUTOTUNE = 4, /* time candidate tile plans per view at creation and keep the fastest;
+                            the choice is kept for the process, so later handles with the same
+                            data-box and kernel sizes on the same device reuse it untimed */
   MVD_FLAG_TENSOR_DFT = 8 /* z passes of the compiled pencil lengths 320 and 288 run their middle
                              16-point DFTs on the tensor cores (TF32, three-term split, FP32
                              accumulation); other lengths stay on the FP32 SIMT path */

@@ -683,6 +683,16 @@ void prepare_kernels(mvd_decon* h) {
 // 384- and 256-thread plane CTAs, are all tried and the fastest plan (one timed view stage
 // each) is kept.  More warps hide more latency; fewer threads leave fewer idle at the stages'
 // last butterfly round, which wins for some plane shapes.
+// The autotuner's choices, kept for the process: an acquisition deconvolves job after job with
+// the same geometry, so only the first job pays for the timing runs.  Keyed by device, data-box
+// size, kernel size and the tensor-core flag.
+struct TunedChoice {
+  int cap, threads;
+  bool generic, ascending;
+};
+std::mutex g_tuned_mu;
+std::map<std::array<int, 8>, TunedChoice> g_tuned;
+
 std::unique_ptr<ConvPlan> plan_view(mvd_decon* h, int v, const int lo[3], const int hi[3], bool autotune,
                                     bool tensor_dft) {
   const auto& k = h->kd[v];
@@ -699,6 +709,17 @@ std::unique_ptr<ConvPlan> plan_view(mvd_decon* h, int v, const int lo[3], const 
     return p;
   };
   if (!autotune) return make(0, false);
+  const std::array<int, 8> key{h->dev, n[0], n[1], n[2], k[0], k[1], k[2], tensor_dft ? 1 : 0};
+  {
+    std::lock_guard<std::mutex> lock(g_tuned_mu);
+    auto it = g_tuned.find(key);
+    if (it != g_tuned.end()) {
+      auto p = make(it->second.cap, it->second.ascending);
+      p->threads_plane = it->second.threads;
+      p->generic = it->second.generic || it->second.ascending;
+      return p;
+    }
+  }
   // one view stage of a candidate (two convolutions' passes), best of 3 after a warm-up
   cudaEvent_t e0, e1;
   MVD_CHECK(cudaEventCreate(&e0));
@@ -726,6 +747,7 @@ std::unique_ptr<ConvPlan> plan_view(mvd_decon* h, int v, const int lo[3], const 
   // ones exist) and at 256 threads, and the generic kernels with every length's radices in
   // ascending order (a second radix plan of the same lengths).
   std::unique_ptr<ConvPlan> best;
+  TunedChoice best_choice{0, kThreads, false, false};
   float best_ms = 1e30f;
   std::vector<std::array<int, 3>> seen;
   for (int cap : {4608, 7168, 10240, 14336}) {
@@ -769,11 +791,14 @@ std::unique_ptr<ConvPlan> plan_view(mvd_decon* h, int v, const int lo[3], const 
     }
     if (ms < best_ms) {
       best_ms = ms;
+      best_choice = TunedChoice{cap, p->threads_plane, p->generic, p->ascending};
       best = std::move(p);
     }
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
+  std::lock_guard<std::mutex> lock(g_tuned_mu);
+  g_tuned[key] = best_choice;
   return best;
 }
 

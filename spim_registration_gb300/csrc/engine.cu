@@ -280,6 +280,21 @@ int plane_cap() {
   return cap;
 }
 
+static bool plane_cap_from_env() {
+  const char* e = std::getenv("MVD_PLANE_CAP");
+  const int v = e ? std::atoi(e) : 0;
+  return v >= 256 && v <= kPlaneCap;
+}
+
+int plane_limit() { return plane_cap_from_env() ? plane_cap() : kPlaneCap; }
+
+double plane_cost_factor(int tx, int ty, long long plane) {
+  if (plane_cap_from_env()) return 1.0;
+  double f = plane > kPlaneCapDefault ? 1.12 : 1.0;
+  if (!compiled_plane_shape(tx, ty)) f *= 1.3;
+  return f;
+}
+
 int plane_threads() {
   static int t = [] {
     const char* e = std::getenv("MVD_PLANE_THREADS");
@@ -382,12 +397,17 @@ std::unique_ptr<ConvPlan> make_conv_plan(PlanTable& pt, int nx, int ny, int nz, 
   auto oz = opts(nz, kz, false, kPlaneCap / kZPitch, opt.force_tz);
   double best = 1e300;
   AxisTiles bx, by, bz;
+  // an explicit budget (the autotuner's candidates) is a hard limit; the default plan weighs
+  // the plane size and the compiled shapes (plane_cost_factor)
+  const int limit = opt.cap > 0 ? opt.cap : plane_limit();
   for (auto& a : ox)
     for (auto& b : oy) {
-      if ((long long)row_pitch(a.T / 2) * b.T > (opt.cap > 0 ? opt.cap : plane_cap())) continue;
+      const long long plane = (long long)row_pitch(a.T / 2) * b.T;
+      if (plane > limit) continue;
+      const double factor = opt.cap > 0 ? 1.0 : plane_cost_factor(a.T, b.T, plane);
       for (auto& c : oz) {
         const double ntiles = (double)a.n * b.n * c.n;
-        const double cost = ntiles * a.T * b.T * c.T * (1.0 + 1e-3 * ntiles);
+        const double cost = ntiles * a.T * b.T * c.T * (1.0 + 1e-3 * ntiles) * factor;
         if (cost < best) {
           best = cost;
           bx = a;

@@ -138,6 +138,15 @@ std::unique_ptr<ConvPlan> make_conv_plan(PlanTable& pt, int nx, int ny, int nz, 
 
 // Planner's budget for one plane buffer (complex values).
 int plane_cap();
+// The default planner's limits: the largest plane buffer it considers (complex values), and
+// the relative cost it gives a tile shape whose plane buffer holds `plane` complex values.
+// Planes beyond two CTAs per SM (kPlaneCapDefault) cost 1.12 (one CTA per SM: the plane passes
+// measured 16% slower at one 1024-thread CTA than at two 512-thread CTAs per SM), shapes without
+// compile-time-shaped kernels 1.3 (the compiled ones measured 28-33% faster per launch).  With
+// MVD_PLANE_CAP set, that budget is a hard limit and every shape costs the same.
+int plane_limit();
+double plane_cost_factor(int tx, int ty, long long plane);
+bool compiled_plane_shape(int tx, int ty);
 // Default CTA size of the plane kernels (MVD_PLANE_THREADS overrides it).
 int plane_threads();
 // Whether compiled tile shapes use their compile-time-shaped plane kernels (MVD_FIXED_PLANES=0

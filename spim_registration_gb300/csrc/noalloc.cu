@@ -59,8 +59,8 @@ struct Axis {
   int T, n, E;
 };
 
-// tile choice: the smallest padded volume over smooth tile sizes whose planes fit the plane
-// budget plane_cap() (the allocating path's planner and budget, so both pick the same tiles)
+// tile choice: the allocating path's default rule (plane_limit, plane_cost_factor), so both
+// pick the same tiles
 std::vector<Axis> options(int size, int k, bool even, int tmax) {
   std::vector<Axis> out;
   int last = -1;
@@ -140,10 +140,12 @@ extern "C" int mvd_convolve3d_device_noalloc(const float* in, float* out, const 
     Axis bx{}, by{}, bz{};
     for (auto& a : ox)
       for (auto& b : oy) {
-        if ((long long)row_pitch(a.T / 2) * b.T > plane_cap()) continue;
+        const long long plane = (long long)row_pitch(a.T / 2) * b.T;
+        if (plane > plane_limit()) continue;
+        const double factor = plane_cost_factor(a.T, b.T, plane);
         for (auto& c : oz) {
           const double nt = (double)a.n * b.n * c.n;
-          const double cost = nt * a.T * b.T * c.T * (1.0 + 1e-3 * nt);
+          const double cost = nt * a.T * b.T * c.T * (1.0 + 1e-3 * nt) * factor;
           if (cost < best) {
             best = cost;
             bx = a;

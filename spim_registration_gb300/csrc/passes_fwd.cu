@@ -47,6 +47,14 @@ static bool launch_fwd_fixed(int tx, int ty, int threads, PlanTable& pt, const T
   return false;
 }
 
+bool compiled_plane_shape(int tx, int ty) {
+#define MVD_SHAPE_Q(SX, SY, ST) \
+  if (tx == SX && ty == SY) return true;
+  MVD_FIXED_PLANE_SHAPES(MVD_SHAPE_Q)
+#undef MVD_SHAPE_Q
+  return false;
+}
+
 int compiled_plane_threads(const ConvPlan& p) {
 #define MVD_SHAPE_T(SX, SY, ST) \
   if (p.ax.T == SX && p.ay.T == SY) return ST;
