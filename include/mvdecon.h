@@ -162,8 +162,9 @@ int mvd_get_plan(mvd_decon* h, int view, int* tiles_xyz, int* tile_xyz, int* eff
 
 /* The kernels the view's plan runs (chosen by MVD_FLAG_AUTOTUNE, else the defaults): *threads =
  * the plane kernels' CTA size; *variant bit 0 = compile-time-shaped kernels, bit 1 = radices in
- * ascending order (generic kernels), bit 2 = tensor-core middle DFT stage in the z pass.  No
- * counterpart in the reference. */
+ * ascending order (generic kernels), bit 2 = tensor-core middle DFT stage in the z pass, bit 3 =
+ * in-place plane kernels staged through tensor memory (two CTAs per SM).  No counterpart in the
+ * reference. */
 int mvd_get_plan_variant(mvd_decon* h, int view, int* threads, int* variant);
 
 /* The cudaStream_t the handle enqueues on (for events recorded by the caller). */

@@ -688,7 +688,7 @@ void prepare_kernels(mvd_decon* h) {
 // size, kernel size and the tensor-core flag.
 struct TunedChoice {
   int cap, threads;
-  bool generic, ascending;
+  bool generic, ascending, staged;
 };
 std::mutex g_tuned_mu;
 std::map<std::array<int, 8>, TunedChoice> g_tuned;
@@ -717,6 +717,7 @@ std::unique_ptr<ConvPlan> plan_view(mvd_decon* h, int v, const int lo[3], const 
       auto p = make(it->second.cap, it->second.ascending);
       p->threads_plane = it->second.threads;
       p->generic = it->second.generic || it->second.ascending;
+      p->staged = it->second.staged;
       return p;
     }
   }
@@ -747,7 +748,7 @@ std::unique_ptr<ConvPlan> plan_view(mvd_decon* h, int v, const int lo[3], const 
   // ones exist) and at 256 threads, and the generic kernels with every length's radices in
   // ascending order (a second radix plan of the same lengths).
   std::unique_ptr<ConvPlan> best;
-  TunedChoice best_choice{0, kThreads, false, false};
+  TunedChoice best_choice{0, kThreads, false, false, false};
   float best_ms = 1e30f;
   std::vector<std::array<int, 3>> seen;
   for (int cap : {4608, 7168, 10240, 14336}) {
@@ -759,20 +760,25 @@ std::unique_ptr<ConvPlan> plan_view(mvd_decon* h, int v, const int lo[3], const 
     MVD_CHECK(cudaMemsetAsync(otf.p, 0, otf.bytes, h->stream));
     struct Variant {
       int threads;
-      bool generic;
+      bool generic, staged;
     };
-    // the tensor-core z pass runs with the compiled kernels only: with it asked for, they are
-    // the one variant timed (the generic and ascending-radix candidates would drop it)
-    std::vector<Variant> variants{{kThreads, false}};
+    // the tensor-core z pass runs with the compiled kernels only: with it asked for, they (and
+    // their in-place variant) are the variants timed (the generic and ascending-radix
+    // candidates would drop it)
+    std::vector<Variant> variants{{kThreads, false, false}};
+    p->staged = true;
+    if (has_staged_kernels(*p)) variants.push_back({kThreads, false, true});
+    p->staged = false;
     if (!tensor_dft) {
-      variants.push_back({256, true});
-      if (has_compiled_kernels(*p)) variants.push_back({kThreads, true});
+      variants.push_back({256, true, false});
+      if (has_compiled_kernels(*p)) variants.push_back({kThreads, true, false});
     }
     float ms = 1e30f;
     Variant bv = variants[0];
     for (const Variant& var : variants) {
       p->threads_plane = var.threads;
       p->generic = var.generic;
+      p->staged = var.staged;
       const float t = time_stage(*p, otf, spec);
       if (t < ms) {
         ms = t;
@@ -781,6 +787,7 @@ std::unique_ptr<ConvPlan> plan_view(mvd_decon* h, int v, const int lo[3], const 
     }
     p->threads_plane = bv.threads;
     p->generic = bv.generic;
+    p->staged = bv.staged;
     if (!tensor_dft) {
       auto asc = make(cap, true);
       const float t_asc = time_stage(*asc, otf, spec);
@@ -791,7 +798,7 @@ std::unique_ptr<ConvPlan> plan_view(mvd_decon* h, int v, const int lo[3], const 
     }
     if (ms < best_ms) {
       best_ms = ms;
-      best_choice = TunedChoice{cap, p->threads_plane, p->generic, p->ascending};
+      best_choice = TunedChoice{cap, p->threads_plane, p->generic, p->ascending, p->staged};
       best = std::move(p);
     }
   }
@@ -1121,10 +1128,11 @@ extern "C" int mvd_get_plan_variant(mvd_decon* h, int view, int* threads, int* v
   if (view < 0 || view >= h->V) return fail(MVD_ERR_ARG, "view out of range");
   const ConvPlan& p = *h->plans[view];
   const bool compiled = !p.generic && has_compiled_kernels(p) && p.threads_plane == kThreads;
-  if (threads) *threads = compiled && compiled_plane_threads(p) ? compiled_plane_threads(p) : p.threads_plane;
+  const bool staged = compiled && p.staged && has_staged_kernels(p);
+  if (threads) *threads = staged ? 512 : compiled && compiled_plane_threads(p) ? compiled_plane_threads(p) : p.threads_plane;
   if (variant)
     *variant = (compiled ? 1 : 0) | (p.ascending ? 2 : 0) |
-               (p.tensor_dft && !p.generic && tensor_dft_supported(p.az.T) ? 4 : 0);
+               (p.tensor_dft && !p.generic && tensor_dft_supported(p.az.T) ? 4 : 0) | (staged ? 8 : 0);
   return MVD_OK;
 }
 

@@ -290,7 +290,8 @@ int plane_limit() { return plane_cap_from_env() ? plane_cap() : kPlaneCap; }
 
 double plane_cost_factor(int tx, int ty, long long plane) {
   if (plane_cap_from_env()) return 1.0;
-  double f = plane > kPlaneCapDefault ? 1.12 : 1.0;
+  const bool two_per_sm = plane <= kPlaneCapDefault || (use_staged_planes() && staged_plane_shape(tx, ty));
+  double f = two_per_sm ? 1.0 : 1.12;
   if (!compiled_plane_shape(tx, ty)) f *= 1.3;
   return f;
 }
@@ -360,6 +361,14 @@ bool volume_box_map(const float* base, int nx, int ny, int nz, int w, int h, CUt
 bool use_l2_prefetch() {
   static bool on = [] {
     const char* e = std::getenv("MVD_L2_PREFETCH");
+    return !(e && e[0] == '0');
+  }();
+  return on;
+}
+
+bool use_staged_planes() {
+  static bool on = [] {
+    const char* e = std::getenv("MVD_STAGED_PLANES");
     return !(e && e[0] == '0');
   }();
   return on;
@@ -455,6 +464,7 @@ std::unique_ptr<ConvPlan> make_conv_plan(PlanTable& pt, int nx, int ny, int nz, 
   p.threads_plane = opt.threads > 0 ? opt.threads : plane_threads();
   p.ascending = opt.ascending;
   p.generic = opt.generic || opt.ascending;  // compiled kernels hold the descending order
+  p.staged = use_staged_planes();
   p.smem_z = 2 * (size_t)bz.T * kZPitch * sizeof(float2);
   fill_items(p);
   p.upload();

@@ -112,6 +112,7 @@ struct ConvPlan {
   bool tensor_dft = false;             // z pass with its middle DFT stage on the tensor cores (if compiled)
   bool ascending = false;              // radices of every length in ascending order
   bool generic = false;                // run the generic kernels even where a compiled shape exists
+  bool staged = false;                 // large compiled planes: in-place kernels, two CTAs per SM
   DevBuf d_tiles, d_items_fwd, d_items_inv, d_items_z;
   // one tile of this shape at the origin and its work items: the OTF build's tables
   DevBuf d_otf_tile, d_otf_fwd, d_otf_z;
@@ -142,7 +143,8 @@ int plane_cap();
 // the relative cost it gives a tile shape whose plane buffer holds `plane` complex values.
 // Planes beyond two CTAs per SM (kPlaneCapDefault) cost 1.12 (one CTA per SM: the plane passes
 // measured 16% slower at one 1024-thread CTA than at two 512-thread CTAs per SM), shapes without
-// compile-time-shaped kernels 1.3 (the compiled ones measured 28-33% faster per launch).  With
+// compile-time-shaped kernels 1.3 (the compiled ones measured 28-33% faster per launch); the
+// large shapes with in-place kernels run two CTAs per SM and take no plane-size factor.  With
 // MVD_PLANE_CAP set, that budget is a hard limit and every shape costs the same.
 int plane_limit();
 double plane_cost_factor(int tx, int ty, long long plane);
@@ -152,6 +154,11 @@ int plane_threads();
 // Whether compiled tile shapes use their compile-time-shaped plane kernels (MVD_FIXED_PLANES=0
 // selects the generic kernels everywhere).
 bool use_fixed_planes();
+// Whether plans of the large compiled shapes run the in-place plane kernels (two CTAs per SM;
+// MVD_STAGED_PLANES=0 selects the two-buffer kernels; the autotuner times both either way), and
+// whether a shape has them.
+bool use_staged_planes();
+bool staged_plane_shape(int tx, int ty);
 // L2 prefetch through tensor maps in the plane kernels (MVD_L2_PREFETCH=0 turns it off).
 bool use_l2_prefetch();
 // Whether pencils of length tz have a tensor-core z pass, and the number of its MMA waits that
@@ -165,6 +172,8 @@ struct ConvPlan;
 // Whether the plan's plane shape or pencil length has compiled kernels, and the CTA size of the
 // compiled plane kernels of its shape (0 if none).
 bool has_compiled_kernels(const ConvPlan& p);
+// Whether the plan's plane shape has in-place (tensor-memory-staged) kernels for its rows.
+bool has_staged_kernels(const ConvPlan& p);
 int compiled_plane_threads(const ConvPlan& p);
 // Tensor map of a float volume [nz][ny][nx] with a (w, h, 1) box (cached); false when the volume
 // does not meet the tensor copy's rules (16-byte aligned base and row stride, box <= 256).

@@ -10,6 +10,7 @@
 
 #include "engine.h"
 #include "fixed_plane.cuh"
+#include "fixed_plane_tm.cuh"
 
 namespace mvd {
 
@@ -29,8 +30,24 @@ int resident_ctas(int per_sm) {
 // size run it at its own size).
 template <class Gather>
 static bool launch_fwd_fixed(int tx, int ty, int threads, PlanTable& pt, const TileDesc* tiles, const int2* items,
-                             int nitems, size_t smem, float2* spec, Gather g, cudaStream_t s) {
+                             int nitems, size_t smem, float2* spec, Gather g, cudaStream_t s, bool staged) {
   if (threads != kThreads || !use_fixed_planes()) return false;
+  if (staged) {
+#define MVD_FWD_TM_CASE(TX, TY)                                                                         \
+    if (tx == TX && ty == TY) {                                                                         \
+      EpiBoxes src;                                                                                     \
+      std::memset(&src, 0, sizeof(src));                                                                \
+      src.count = use_l2_prefetch() &&                                                                  \
+                  volume_box_map(g.v.data, g.v.nx, g.v.ny, g.v.nz, prefetch_box_width(TX), TY, &src.map[0]); \
+      auto k = plane_fwd_tm<Gather, TX, TY>;                                                            \
+      const size_t sm = (size_t)TY * fixed_pitch(TX) * sizeof(float2);                                  \
+      set_smem(k, sm);                                                                                  \
+      k<<<nitems, kTmThreads, sm, s>>>(tiles, items, pt.device(), spec, g, src, resident_ctas(2));      \
+      return true;                                                                                      \
+    }
+    MVD_TM_PLANE_SHAPES(MVD_FWD_TM_CASE)
+#undef MVD_FWD_TM_CASE
+  }
 #define MVD_FWD_CASE(TX, TY, T)                                                                         \
   if (tx == TX && ty == TY) {                                                                           \
     EpiBoxes src;                                                                                       \
@@ -63,6 +80,22 @@ int compiled_plane_threads(const ConvPlan& p) {
   return 0;
 }
 
+bool staged_plane_shape(int tx, int ty) {
+#define MVD_TM_S(SX, SY) \
+  if (tx == SX && ty == SY) return true;
+  MVD_TM_PLANE_SHAPES(MVD_TM_S)
+#undef MVD_TM_S
+  return false;
+}
+
+bool has_staged_kernels(const ConvPlan& p) {
+#define MVD_TM_Q(SX, SY) \
+  if (p.ax.T == SX && p.ay.T == SY) return p.ay.E <= tm_max_rows<SX, SY>();
+  MVD_TM_PLANE_SHAPES(MVD_TM_Q)
+#undef MVD_TM_Q
+  return false;
+}
+
 bool has_compiled_kernels(const ConvPlan& p) {
   if (compiled_plane_threads(p)) return true;
 #define MVD_Z_LEN(SZ) \
@@ -75,10 +108,11 @@ bool has_compiled_kernels(const ConvPlan& p) {
 template <class Gather, bool MASK = false>
 static void launch_fwd_impl(PlanTable& pt, const TileDesc* tiles, const int2* items, int nitems, size_t smem,
                             int threads, int tx, int ty, float2* spec, Gather g, cudaStream_t s,
-                            bool generic = false) {
+                            bool generic = false, bool staged = false) {
   if (nitems == 0) return;
   if (MASK || generic ||
-      !launch_fwd_fixed(tx, ty, threads > 0 ? threads : kThreads, pt, tiles, items, nitems, smem, spec, g, s)) {
+      !launch_fwd_fixed(tx, ty, threads > 0 ? threads : kThreads, pt, tiles, items, nitems, smem, spec, g, s,
+                        staged)) {
     EpiBoxes src;
     std::memset(&src, 0, sizeof(src));
     src.count = !MASK && use_l2_prefetch() &&
@@ -96,7 +130,7 @@ static void launch_fwd_impl(PlanTable& pt, const TileDesc* tiles, const int2* it
 void launch_fwd_mirror(PlanTable& pt, const ConvPlan& p, const float* vol, float2* spec, cudaStream_t s) {
   GatherMirror g{{vol, p.vol[0], p.vol[1], p.vol[2]}};
   launch_fwd_impl(pt, p.d_tiles.as<TileDesc>(), p.d_items_fwd.as<int2>(), (int)p.items_fwd.size(), p.smem_plane,
-                  p.threads_plane, p.ax.T, p.ay.T, spec, g, s, p.generic);
+                  p.threads_plane, p.ax.T, p.ay.T, spec, g, s, p.generic, p.staged);
 }
 
 void launch_fwd_value(PlanTable& pt, const ConvPlan& p, const float* vol, float value, float2* spec,
@@ -104,7 +138,7 @@ void launch_fwd_value(PlanTable& pt, const ConvPlan& p, const float* vol, float 
   GatherValue g = GatherValue::box(vol, p.vol[0], p.vol[1], p.vol[2], value, p.box_lo[0], p.box_lo[1], p.box_lo[2],
                                    p.box_hi[0], p.box_hi[1], p.box_hi[2]);
   launch_fwd_impl(pt, p.d_tiles.as<TileDesc>(), p.d_items_fwd.as<int2>(), (int)p.items_fwd.size(), p.smem_plane,
-                  p.threads_plane, p.ax.T, p.ay.T, spec, g, s, p.generic);
+                  p.threads_plane, p.ax.T, p.ay.T, spec, g, s, p.generic, p.staged);
 }
 
 void launch_fwd_value_items(PlanTable& pt, const ConvPlan& p, const TileDesc* tiles, const int2* items, int nitems,

@@ -4,6 +4,7 @@
 
 #include "engine.h"
 #include "fixed_plane.cuh"
+#include "fixed_plane_tm.cuh"
 
 namespace mvd {
 
@@ -30,6 +31,18 @@ static bool launch_inv_fixed(PlanTable& pt, const ConvPlan& p, const TileDesc* t
   if (threads != kThreads || p.generic || !use_fixed_planes()) return false;
   const int tx = p.ax.T, ty = p.ay.T;
   const EpiBoxes boxes = epilogue_boxes(p, e);
+  if (p.staged && has_staged_kernels(p)) {
+#define MVD_INV_TM_CASE(TX, TY)                                                        \
+    if (tx == TX && ty == TY) {                                                        \
+      auto k = plane_inv_tm<Epi, TX, TY>;                                              \
+      const size_t sm = (size_t)TY * fixed_pitch(TX) * sizeof(float2);                 \
+      set_smem(k, sm);                                                                 \
+      k<<<nitems, kTmThreads, sm, s>>>(tiles, items, pt.device(), spec, e, boxes);     \
+      return true;                                                                     \
+    }
+    MVD_TM_PLANE_SHAPES(MVD_INV_TM_CASE)
+#undef MVD_INV_TM_CASE
+  }
 #define MVD_INV_CASE(TX, TY, T)                                                        \
   if (tx == TX && ty == TY) {                                                          \
     auto k = plane_inv_fixed<Epi, TX, TY, T>;                                          \

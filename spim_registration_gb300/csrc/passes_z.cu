@@ -1,4 +1,5 @@
 // Instantiations and launches of the z-pencil pass (split from engine.cu so the library builds in parallel).
+#include <algorithm>
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
@@ -87,6 +88,17 @@ TcState& tc_state() {
   return st;
 }
 
+// Polls of each bounded MMA wait: 2^22 (far beyond a product's microseconds), or
+// MVD_TC_WAIT_POLLS (>= 0) -- 0 makes every wait give up at once, which is how the failure path
+// (error count, bounded wait for the products in flight, tensor memory freed) is tested.
+int tc_wait_polls() {
+  static int polls = [] {
+    const char* e = std::getenv("MVD_TC_WAIT_POLLS");
+    return (e && *e) ? std::max(0, std::atoi(e)) : (1 << 22);
+  }();
+  return polls;
+}
+
 // The tensor-core z pass for the plan's pencil length, if it has one.
 bool launch_z_tc(PlanTable& pt, const ConvPlan& p, float2* spec, const float2* otf, cudaStream_t s) {
   const int tz = p.az.T;
@@ -97,7 +109,7 @@ bool launch_z_tc(PlanTable& pt, const ConvPlan& p, float2* spec, const float2* o
     const size_t sm = zpass_tc_smem<TZ>();                                                                    \
     set_smem(k, sm);                                                                                          \
     k<<<(int)p.items_z.size(), kZThreads, sm, s>>>(p.d_tiles.as<TileDesc>(), p.d_items_z.as<int2>(), pt.device(), \
-                                                   spec, otf, st.mats, st.failures);                          \
+                                                   spec, otf, st.mats, st.failures, tc_wait_polls());         \
     return true;                                                                                              \
   }
   MVD_TC_Z_LENGTHS(MVD_TC_CASE)

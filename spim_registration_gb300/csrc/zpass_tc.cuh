@@ -13,6 +13,7 @@
 // Results are read back with tcgen05.ld (one butterfly row per thread and 8 complex values per
 // half of the CTA), multiplied by the kernel spectrum in registers and fed to the inverse product.
 //
+// `polls` bounds every wait (the host passes 2^22, or MVD_TC_WAIT_POLLS for the failure test).
 // The CTA: 256 threads, one CTA per SM (the operand tiles take 48 KB of shared memory on top of
 // the two pencil buffers), 64 tensor-memory columns (forward and inverse accumulators).  Every
 // wait on the MMA completion is bounded; a wait that gives up records it in `err`, skips the
@@ -39,7 +40,8 @@ __host__ __device__ constexpr size_t zpass_tc_smem() {
 template <int TZ>
 __global__ void __launch_bounds__(kZThreads, 1)
 zpass_tc(const TileDesc* __restrict__ tiles, const int2* __restrict__ items, const FftPlan* __restrict__ plans,
-         float2* __restrict__ spec, const float2* __restrict__ otf, const float4* __restrict__ dft_mats, int* err) {
+         float2* __restrict__ spec, const float2* __restrict__ otf, const float4* __restrict__ dft_mats, int* err,
+         int polls) {
   constexpr SplitC sp = split_of(TZ);
   static_assert(sp.s == 2 && sp.r[1] == 16, "tensor-core middle stage needs TZ = R0 x 16");
   constexpr int R0 = sp.r[0];
@@ -124,7 +126,7 @@ zpass_tc(const TileDesc* __restrict__ tiles, const int2* __restrict__ items, con
         }
       tc::mma_commit(&bar);
     }
-    const bool ok = tc::mbar_wait(&bar, phase);
+    const bool ok = tc::mbar_wait(&bar, phase, polls);
     phase ^= 1u;
     tc::fence_after_sync();
     return ok;
@@ -176,7 +178,7 @@ zpass_tc(const TileDesc* __restrict__ tiles, const int2* __restrict__ items, con
   }
   if (failed) {
     if (tid == 0) atomicAdd(err, 1);
-    tc::mbar_wait(&bar, phase, 1 << 20);  // the products in flight, once more (bounded)
+    tc::mbar_wait(&bar, phase ^ 1u, 1 << 20);  // the products of the wait that gave up (bounded)
   } else {
     __syncthreads();
     float2* c2 = oth;

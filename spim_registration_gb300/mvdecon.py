@@ -302,7 +302,7 @@ class Deconvolution:
         return dict(tiles=tuple(t), tile=tuple(s), effective=tuple(e), padded_voxels=pv.value,
                     threads=th.value, kernels="compiled" if var.value & 1 else "generic",
                     radix_order="ascending" if var.value & 2 else "descending",
-                    tensor_dft=bool(var.value & 4))
+                    tensor_dft=bool(var.value & 4), staged=bool(var.value & 8))
 
 
 class MVDeconvolution:

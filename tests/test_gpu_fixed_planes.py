@@ -40,8 +40,8 @@ SCRIPT = textwrap.dedent("""
 """)
 
 
-def _run(out, fixed, case="full", cap=None):
-    env = dict(os.environ, MVD_FIXED_PLANES="1" if fixed else "0")
+def _run(out, fixed, case="full", cap=None, staged=False):
+    env = dict(os.environ, MVD_FIXED_PLANES="1" if fixed else "0", MVD_STAGED_PLANES="1" if staged else "0")
     if cap:
         env["MVD_PLANE_CAP"] = str(cap)
     r = subprocess.run([sys.executable, "-c", SCRIPT.format(root=ROOT), out, case], env=env, capture_output=True,
@@ -69,4 +69,16 @@ def test_large_psf_shapes_equal_the_generic_kernels(tmp_path, cap, plane, case):
     assert _run(b, False, case, cap) == shapes
     assert any(t.startswith(plane) for t in shapes), shapes
     assert any(t.endswith("x320") for t in shapes) and (cap == 14336 or any(t.endswith("x288") for t in shapes))
+    np.testing.assert_array_equal(np.load(a), np.load(b))
+
+
+@pytest.mark.parametrize("cap,plane,case", [(14336, "160x160x", "large"), (10240, "192x96x", "large"),
+                                            (14336, "192x135x", "large135")])
+def test_in_place_plane_kernels_equal_the_two_buffer_kernels(tmp_path, cap, plane, case):
+    """The in-place plane kernels (one shared buffer, stages staged through tensor memory, two
+    CTAs per SM) against the two-buffer compiled kernels, bit for bit."""
+    a, b = str(tmp_path / "staged.npy"), str(tmp_path / "two_buffer.npy")
+    shapes = _run(a, True, case, cap, staged=True)
+    assert _run(b, True, case, cap, staged=False) == shapes
+    assert any(t.startswith(plane) for t in shapes), shapes
     np.testing.assert_array_equal(np.load(a), np.load(b))
