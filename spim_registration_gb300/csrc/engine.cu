@@ -231,12 +231,17 @@ static void fill_items(ConvPlan& p) {
     for (int z = t.hz; z < t.hz + t.ez; ++z) p.items_inv.push_back(make_int2(i, z));
     plane_max = std::max(plane_max, t.ty * t.px);
   }
-  for (int b0 = 0; b0 < plane_max; b0 += kZBlock * kZChunk)
-    for (int i = 0; i < (int)p.tiles.size(); ++i) {
-      const int plane = p.tiles[i].ty * p.tiles[i].px;
-      for (int p0 = b0; p0 < std::min(plane, b0 + kZBlock * kZChunk); p0 += kZChunk)
-        p.items_z.push_back(make_int2(i, p0));
-    }
+  auto zitems = [&](std::vector<int2>& out, int chunk) {
+    out.clear();
+    for (int b0 = 0; b0 < plane_max; b0 += kZBlock * kZChunk)
+      for (int i = 0; i < (int)p.tiles.size(); ++i) {
+        const int plane = p.tiles[i].ty * p.tiles[i].px;
+        for (int p0 = b0; p0 < std::min(plane, b0 + kZBlock * kZChunk); p0 += chunk)
+          out.push_back(make_int2(i, p0));
+      }
+  };
+  zitems(p.items_z, kZChunk);
+  zitems(p.items_zw, kZWideChunk);
 }
 
 void ConvPlan::upload() {
@@ -249,6 +254,7 @@ void ConvPlan::upload() {
   up(d_items_fwd, items_fwd);
   up(d_items_inv, items_inv);
   up(d_items_z, items_z);
+  up(d_items_zw, items_zw);
   // OTF build tables: one tile of this shape covering [0, T) with its full region effective
   if (!tiles.empty()) {
     TileDesc t = tiles[0];

@@ -105,6 +105,7 @@ struct ConvPlan {
   AxisTiles ax, ay, az;
   std::vector<TileDesc> tiles;         // host copy
   std::vector<int2> items_fwd, items_inv, items_z;
+  std::vector<int2> items_zw;          // z items of kZWideChunk pencils (the in-place z pass)
   long long spec_elems = 0;            // complex elements of all tile spectra
   long long otf_elems = 0;             // complex elements of one OTF (all tiles share the shape)
   size_t smem_plane = 0, smem_z = 0;
@@ -113,7 +114,7 @@ struct ConvPlan {
   bool ascending = false;              // radices of every length in ascending order
   bool generic = false;                // run the generic kernels even where a compiled shape exists
   bool staged = false;                 // large compiled planes: in-place kernels, two CTAs per SM
-  DevBuf d_tiles, d_items_fwd, d_items_inv, d_items_z;
+  DevBuf d_tiles, d_items_fwd, d_items_inv, d_items_z, d_items_zw;
   // one tile of this shape at the origin and its work items: the OTF build's tables
   DevBuf d_otf_tile, d_otf_fwd, d_otf_z;
   int n_otf_fwd = 0, n_otf_z = 0;

@@ -383,6 +383,78 @@ __host__ __device__ constexpr int zpass_fixed_occ(int TZ) {
   return 3 * 2 * TZ * kZPitch * 8 <= 227 * 1024 ? 3 : 2;
 }
 
+// Loader of the inverse stage after the in-place middle stage of zpass_ip: butterfly j reads the
+// R consecutive elements j R ... j R + R - 1 of its pencil (rows of PITCH complex).
+template <int PITCH>
+struct ZRowsLoad {
+  const float2* p;
+  template <int R>
+  __device__ __forceinline__ void get(int batch, int j, int, float2* v) const {
+    const float2* q = p + batch + j * R * PITCH;
+#pragma unroll
+    for (int r = 0; r < R; ++r) v[r] = q[r * PITCH];
+  }
+};
+
+// zpass_fixed for two-stage pencil lengths TZ = R0 x R1 with ONE shared buffer, CH pencils per
+// CTA of T threads.  The middle stage (forward radix R1, product with the OTF, inverse radix
+// R1) writes each butterfly's results back to the positions it read them from (j + r R0),
+// instead of the Stockham order (j R1 + r): no other thread touches those positions, so the
+// stage needs neither a second buffer nor a barrier between its loads and stores.  Element
+// e = a R1 + c of the Stockham order then sits at a + c R0, so the inverse radix-R0 stage, whose
+// butterfly j wants elements j + r R1 (a = r, c = j), reads positions j R0 + r (ZRowsLoad).
+// Arithmetic, twiddles and the order of operations are zpass_fixed's, so results are
+// bit-identical to it.
+//
+// The host runs it with 32 pencils per CTA (kZWideChunk), 256 threads and two CTAs per SM:
+// the one buffer (TZ x 33 complex, 84 KB for 320) takes what two 16-pencil buffers took, and
+// each z slice of a chunk is one 256-byte row in HBM instead of 128 bytes.  On the 512x512x256
+// workload the z pass took 2.79 ms per iteration against 3.36 ms for the two-buffer kernel.  16
+// pencils with four CTAs per SM (64 registers) took 3.80 ms, 32 pencils with 512 threads 3.83,
+// 64 pencils with 512 threads and one CTA 3.16.
+template <int TZ, int CH, int T, int OCC>
+__global__ void __launch_bounds__(T, OCC)
+zpass_ip(const TileDesc* __restrict__ tiles, const int2* __restrict__ items, const FftPlan* __restrict__ plans,
+         float2* __restrict__ spec, const float2* __restrict__ otf) {
+  constexpr SplitC sp = split_of(TZ);
+  static_assert(sp.s == 2, "the in-place z pass is written for two-stage pencil lengths");
+  constexpr int R0 = sp.r[0];
+  constexpr int R1 = sp.r[1];
+  constexpr int PITCH = CH + 1;
+  extern __shared__ float2 sm[];
+  const int2 it = items[blockIdx.x];
+  const TileDesc t = tiles[it.x];
+  const int p0 = it.y;
+  const int plane = t.ty * t.px;
+  const int count = min(CH, plane - p0);
+  const float2* tw = plans[t.plan_z].tw;
+  const SmemC<PITCH, 1, false> buf{sm};
+  PencilRef g{spec + t.spec_off + p0, plane};
+  OtfMul mul{otf + t.otf_off + p0, plane};
+  // forward stage 0 straight from the pencils: butterfly j's outputs at j R0 + r
+  stage_c<R0, TZ, 1, false, false, T>(count, tw, g, buf);
+  __syncthreads();
+  {
+    const int nb = count * R0;  // R0 butterflies of radix R1 per pencil
+    for (int b = threadIdx.x; b < nb; b += T) {
+      const int j = b / count;
+      const int batch = b - j * count;
+      float2 v[R1];
+      buf.template get<R1>(batch, j, R0, v);
+      if (j != 0) {
+#pragma unroll
+        for (int r = 1; r < R1; ++r) v[r] = cmul(v[r], __ldg(tw + r * j));
+      }
+      Dft<R1, false>::run(v);
+      mul.template apply<R1>(batch, j, R0, v);
+      Dft<R1, true>::run(v);
+      buf.template put<R1>(batch, j, R0, v);
+    }
+  }
+  __syncthreads();
+  stage_c<R0, TZ, R1, true, false, T>(count, tw, ZRowsLoad<PITCH>{sm}, g);
+}
+
 // Pencil lengths with compiled z-pass kernels: the 4-view 256x256x192 workload's (240, 216)
 // and the 512x512x256 workload's (320, 288).
 #define MVD_FIXED_Z_LENGTHS(X) \

@@ -52,6 +52,7 @@ constexpr int kPlaneCap = 14336; // complex values of one shared-memory buffer (
 constexpr int kPlaneCapDefault = 7168;  // planner default: two CTAs per SM (measured faster)
 constexpr int kZChunk = 16;      // pencils per z-pass CTA (16 complex = one 128-byte line)
 constexpr int kZPitch = kZChunk + 1;
+constexpr int kZWideChunk = 32;  // pencils per CTA of the in-place compiled z pass (256-byte rows)
 
 // Row pitch (complex values, odd) that holds a half-spectrum row of px = M + 1 values and
 // the skewed layout i + i/16 of a length-M row between the first two row stages.

@@ -22,12 +22,30 @@ static int z_occupancy() {
   return occ;
 }
 
+// The in-place z pass (zpass_ip, kZWideChunk pencils per CTA) for the compiled two-stage
+// lengths; MVD_Z_INPLACE=0 selects the two-buffer kernel.
+static bool z_in_place() {
+  static bool on = [] {
+    const char* e = std::getenv("MVD_Z_INPLACE");
+    return !(e && e[0] == '0');
+  }();
+  return on;
+}
+
 // The compile-time-length z pass for the plan's pencil length, if one is compiled.
 static bool launch_z_fixed(PlanTable& pt, const ConvPlan& p, float2* spec, const float2* otf, cudaStream_t s) {
   if (p.generic || !use_fixed_planes() || z_occupancy() != 3) return false;
   const int tz = p.az.T;
 #define MVD_Z_CASE(TZ)                                                                                       \
   if (tz == TZ) {                                                                                            \
+    if (z_in_place()) {                                                                                      \
+      auto k = zpass_ip<TZ, kZWideChunk, kZThreads, 2>;                                                      \
+      const size_t sm = (size_t)TZ * (kZWideChunk + 1) * sizeof(float2);                                     \
+      set_smem(k, sm);                                                                                       \
+      k<<<(int)p.items_zw.size(), kZThreads, sm, s>>>(p.d_tiles.as<TileDesc>(), p.d_items_zw.as<int2>(),    \
+                                                      pt.device(), spec, otf);                              \
+      return true;                                                                                           \
+    }                                                                                                        \
     auto k = zpass_fixed<TZ, zpass_fixed_occ(TZ)>;                                                         \
     set_smem(k, p.smem_z);                                                                                   \
     k<<<(int)p.items_z.size(), kZThreads, p.smem_z, s>>>(p.d_tiles.as<TileDesc>(), p.d_items_z.as<int2>(), \

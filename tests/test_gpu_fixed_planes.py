@@ -40,8 +40,9 @@ SCRIPT = textwrap.dedent("""
 """)
 
 
-def _run(out, fixed, case="full", cap=None, staged=False):
-    env = dict(os.environ, MVD_FIXED_PLANES="1" if fixed else "0", MVD_STAGED_PLANES="1" if staged else "0")
+def _run(out, fixed, case="full", cap=None, staged=False, z_in_place=True):
+    env = dict(os.environ, MVD_FIXED_PLANES="1" if fixed else "0", MVD_STAGED_PLANES="1" if staged else "0",
+               MVD_Z_INPLACE="1" if z_in_place else "0")
     if cap:
         env["MVD_PLANE_CAP"] = str(cap)
     r = subprocess.run([sys.executable, "-c", SCRIPT.format(root=ROOT), out, case], env=env, capture_output=True,
@@ -81,4 +82,16 @@ def test_in_place_plane_kernels_equal_the_two_buffer_kernels(tmp_path, cap, plan
     shapes = _run(a, True, case, cap, staged=True)
     assert _run(b, True, case, cap, staged=False) == shapes
     assert any(t.startswith(plane) for t in shapes), shapes
+    np.testing.assert_array_equal(np.load(a), np.load(b))
+
+
+@pytest.mark.parametrize("case,lengths", [("full", ("x240", "x216")), ("large", ("x320", "x288"))])
+def test_in_place_z_pass_equals_the_two_buffer_z_pass(tmp_path, case, lengths):
+    """The one-buffer z pass (middle stage written back in place, four CTAs per SM) against the
+    two-buffer compiled z pass, bit for bit, on the compiled pencil lengths of both workloads."""
+    a, b = str(tmp_path / "in_place.npy"), str(tmp_path / "two_buffer.npy")
+    cap = 10240 if case == "large" else None
+    shapes = _run(a, True, case, cap, staged=True)
+    assert _run(b, True, case, cap, staged=True, z_in_place=False) == shapes
+    assert any(t.endswith(lengths) for t in shapes), shapes
     np.testing.assert_array_equal(np.load(a), np.load(b))
