@@ -119,7 +119,7 @@ struct DeviceCtx {
   }
 };
 
-// MVD_TRACE=1 prints the duration of mvd_create's phases to stderr.
+// MVD_TRACE=1 prints the duration of the phases of mvd_create and mvd_get_psi to stderr.
 struct PhaseTrace {
   bool on;
   std::chrono::steady_clock::time_point t0;
@@ -135,7 +135,7 @@ struct PhaseTrace {
     auto th = std::chrono::steady_clock::now();
     cudaStreamSynchronize(s);
     auto t1 = std::chrono::steady_clock::now();
-    std::fprintf(stderr, "[mvd_create] %-28s %8.2f ms (host %.2f ms)\n", what,
+    std::fprintf(stderr, "[mvd] %-32s %8.2f ms (host %.2f ms)\n", what,
                  std::chrono::duration<double, std::milli>(t1 - t0).count(),
                  std::chrono::duration<double, std::milli>(th - t0).count());
     t0 = t1;
@@ -898,9 +898,10 @@ extern "C" int mvd_create(mvd_decon** out, int devCUDA, const int* dims, int num
   };
   if (async_src) copy_inputs();
   prepare_kernels(h.get());
+  trace.mark("kernel preparation");
   if (!async_src) copy_inputs();
   up.join();
-  trace.mark("upload with kernel preparation");
+  trace.mark("input upload (rest of it)");
   h->psi.alloc(nb);
   h->q.alloc(nb);
   MVD_CHECK(cudaMemsetAsync(h->psi.p, 0, nb, h->stream));
@@ -1037,14 +1038,18 @@ extern "C" int mvd_get_psi(mvd_decon* h, float* psi, int masked) {
   MVD_CHECK(cudaSetDevice(h->dev));
   const size_t nb = h->N * sizeof(float);
   if (masked) {
+    PhaseTrace trace(h->stream);
+    trace.mark("get_psi: pending work");
     // the quotient buffer is idle between view stages (every stage rewrites it before use):
     // the masked copy is staged there instead of in a fresh allocation
     MVD_CHECK(cudaMemcpyAsync(h->q.p, h->psi.p, nb, cudaMemcpyDeviceToDevice, h->stream));
     std::vector<const float*> vp;
     for (int v = 0; v < h->V; ++v) vp.push_back(h->img[v].as<float>());
     dev_mask(h->q.as<float>(), vp.data(), h->V, h->N, h->stream);
+    trace.mark("get_psi: mask");
     MVD_CHECK(cudaMemcpyAsync(psi, h->q.p, nb, cudaMemcpyDeviceToHost, h->stream));
     MVD_CHECK(cudaStreamSynchronize(h->stream));
+    trace.mark("get_psi: download");
   } else {
     MVD_CHECK(cudaMemcpyAsync(psi, h->psi.p, nb, cudaMemcpyDeviceToHost, h->stream));
     MVD_CHECK(cudaStreamSynchronize(h->stream));
