@@ -396,6 +396,21 @@ struct ZRowsLoad {
   }
 };
 
+// Store of the inverse z stage that keeps only the tile's effective slices [z0, z1): the inverse
+// plane pass reads no other slice of a convolution's spectrum.
+struct PencilEffectiveStore {
+  float2* p;
+  int plane, z0, z1;
+  template <int R>
+  __device__ __forceinline__ void put(int batch, int base, int Ns, const float2* v) const {
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      const int z = base + r * Ns;
+      if (z >= z0 && z < z1) p[z * plane + batch] = v[r];
+    }
+  }
+};
+
 // zpass_fixed for two-stage pencil lengths TZ = R0 x R1 with ONE shared buffer, CH pencils per
 // CTA of T threads.  The middle stage (forward radix R1, product with the OTF, inverse radix
 // R1) writes each butterfly's results back to the positions it read them from (j + r R0),
@@ -403,8 +418,9 @@ struct ZRowsLoad {
 // stage needs neither a second buffer nor a barrier between its loads and stores.  Element
 // e = a R1 + c of the Stockham order then sits at a + c R0, so the inverse radix-R0 stage, whose
 // butterfly j wants elements j + r R1 (a = r, c = j), reads positions j R0 + r (ZRowsLoad).
-// Arithmetic, twiddles and the order of operations are zpass_fixed's, so results are
-// bit-identical to it.
+// Arithmetic, twiddles and the order of operations are zpass_fixed's, so the effective slices
+// are bit-identical to its output; the halo slices (outside [hz, hz + ez)), which the inverse
+// plane pass never reads, are not stored.
 //
 // The host runs it with 32 pencils per CTA (kZWideChunk), 256 threads and two CTAs per SM:
 // the one buffer (TZ x 33 complex, 84 KB for 320) takes what two 16-pencil buffers took, and
@@ -452,7 +468,9 @@ zpass_ip(const TileDesc* __restrict__ tiles, const int2* __restrict__ items, con
     }
   }
   __syncthreads();
-  stage_c<R0, TZ, R1, true, false, T>(count, tw, ZRowsLoad<PITCH>{sm}, g);
+  // the inverse plane pass reads the effective slices only: the halo slices are not stored
+  stage_c<R0, TZ, R1, true, false, T>(count, tw, ZRowsLoad<PITCH>{sm},
+                                      PencilEffectiveStore{g.p, plane, t.hz, t.hz + t.ez});
 }
 
 // Pencil lengths with compiled z-pass kernels: the 4-view 256x256x192 workload's (240, 216)
