@@ -169,9 +169,9 @@ def make_problem(workload, volume=None):
 def bytes_per_iteration(dec, n_views, n_voxels):
     """Algorithmic HBM bytes of one fused iteration per pass kind, from the live tile plans.
     Per view, with P the tile voxels, H the complex values of the tiles' half spectra and N the
-    volume's voxels: forward plane pass 4 P + 8 H and z pass 16 H + one OTF read, each twice
-    (two convolutions); inverse pass with the quotient 8 H_eff + 8 N; inverse pass with the
-    update 8 H_eff + 12 N."""
+    volume's voxels: forward plane pass 4 P + 8 H and z pass 8 H + 8 H_eff + one OTF read (it
+    reads every slice and stores the effective ones), each twice (two convolutions); inverse
+    pass with the quotient 8 H_eff + 8 N; inverse pass with the update 8 H_eff + 12 N."""
     out = {"plane_fwd": 0, "zpass": 0, "plane_inv_quotient": 0, "plane_inv_update": 0}
     for v in range(n_views):
         p = dec.plan(v)
@@ -184,8 +184,9 @@ def bytes_per_iteration(dec, n_views, n_voxels):
         Heff = nt * half * min(ez, tz)
         # forward plane: gather P reals, write H complex (x2 convolutions)
         out["plane_fwd"] += 2 * (4 * P + 8 * H)
-        # z pass: read H, write H, read the OTF once (all tiles of a view share its shape) (x2)
-        out["zpass"] += 2 * (16 * H + 8 * half * tz)
+        # z pass: read H, write the effective slices, read the OTF once (all tiles of a view
+        # share its shape) (x2)
+        out["zpass"] += 2 * (8 * H + 8 * Heff + 8 * half * tz)
         # inverse plane: read effective spectrum slices; quotient reads img, writes q
         out["plane_inv_quotient"] += 8 * Heff + 8 * n_voxels
         # update reads psi, weight, writes psi

@@ -361,8 +361,9 @@ zpass_fixed(const TileDesc* __restrict__ tiles, const int2* __restrict__ items, 
   float2* oth = sm + TZ * kZPitch;
   PencilRef g{spec + t.spec_off + p0, plane};
   OtfMul mul{otf + t.otf_off + p0, plane};
+  const PencilEffectiveStore ge{g.p, plane, t.hz, t.hz + t.ez};  // the inverse pass's slices only
   if constexpr (sp.s == 1) {
-    zmid_c<sp.r[0], TZ, kZThreads>(count, tw, g, mul, g);
+    zmid_c<sp.r[0], TZ, kZThreads>(count, tw, g, mul, ge);
   } else {
     // forward stage 0 straight from the pencils into `cur`, then the shared stages
     stage_c<sp.r[0], TZ, 1, false, false, kZThreads>(count, tw, g, SmemC<kZPitch, 1, false>{cur});
@@ -373,7 +374,7 @@ zpass_fixed(const TileDesc* __restrict__ tiles, const int2* __restrict__ items, 
     float2* tmp = cur;
     cur = oth;
     oth = tmp;
-    z_inv_stages<TZ, 1, kZThreads>(count, tw, g, cur, oth);
+    z_inv_stages<TZ, 1, kZThreads>(count, tw, ge, cur, oth);
   }
 }
 
@@ -393,21 +394,6 @@ struct ZRowsLoad {
     const float2* q = p + batch + j * R * PITCH;
 #pragma unroll
     for (int r = 0; r < R; ++r) v[r] = q[r * PITCH];
-  }
-};
-
-// Store of the inverse z stage that keeps only the tile's effective slices [z0, z1): the inverse
-// plane pass reads no other slice of a convolution's spectrum.
-struct PencilEffectiveStore {
-  float2* p;
-  int plane, z0, z1;
-  template <int R>
-  __device__ __forceinline__ void put(int batch, int base, int Ns, const float2* v) const {
-#pragma unroll
-    for (int r = 0; r < R; ++r) {
-      const int z = base + r * Ns;
-      if (z >= z0 && z < z1) p[z * plane + batch] = v[r];
-    }
   }
 };
 

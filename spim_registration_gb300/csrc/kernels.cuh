@@ -476,6 +476,21 @@ struct PencilRef {  // pencil element: batch = pencil in the chunk, i = z (32-bi
   }
 };
 
+// Store of a convolution's last inverse z stage that keeps only the tile's effective slices
+// [z0, z1): the inverse plane pass reads no other slice of the spectrum.
+struct PencilEffectiveStore {
+  float2* p;
+  int plane, z0, z1;
+  template <int R>
+  __device__ __forceinline__ void put(int batch, int base, int Ns, const float2* v) const {
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      const int z = base + r * Ns;
+      if (z >= z0 && z < z1) p[z * plane + batch] = v[r];
+    }
+  }
+};
+
 struct PencilScaledStore {
   float2* p;
   int plane;
@@ -713,8 +728,8 @@ plane_inv_kernel(const TileDesc* __restrict__ tiles, const int2* __restrict__ it
   epi.finish();
 }
 
-// MODE 0: forward z, multiply by the OTF, inverse z.  MODE 1: forward z and scale (OTF build,
-// spectra of the PSF gradient).  MODE 2: inverse z only.
+// MODE 0: forward z, multiply by the OTF, inverse z (only the effective slices stored).
+// MODE 1: forward z and scale (OTF build, spectra of the PSF gradient).  MODE 2: inverse z only.
 // OCC: CTAs per SM the register allocation is sized for.
 template <int MODE, int OCC = 2>
 __global__ void __launch_bounds__(kZThreads, OCC)
@@ -743,8 +758,9 @@ zpass_kernel(const TileDesc* __restrict__ tiles, const int2* __restrict__ items,
     return;
   }
   OtfMul mul{otf + t.otf_off + p0, plane};
+  const PencilEffectiveStore ge{g.p, plane, t.hz, t.hz + t.ez};
   if (ns == 1) {
-    zmid(__ldg(&pz->radix[0]), n, count, tw, g, mul, g);
+    zmid(__ldg(&pz->radix[0]), n, count, tw, g, mul, ge);
     return;
   }
   // forward stages 0 .. ns-2
@@ -775,7 +791,7 @@ zpass_kernel(const TileDesc* __restrict__ tiles, const int2* __restrict__ items,
   for (int i = 1; i < ns; ++i) {
     const int R = __ldg(&pz->radix[ns - 1 - i]);
     if (i == ns - 1) {
-      stage<true, false>(R, n, Ns, count, tw, Smem{cur, kZPitch, 1, 0}, g);
+      stage<true, false>(R, n, Ns, count, tw, Smem{cur, kZPitch, 1, 0}, ge);
     } else {
       stage<true, false>(R, n, Ns, count, tw, Smem{cur, kZPitch, 1, 0}, Smem{oth, kZPitch, 1, 0});
       __syncthreads();

@@ -183,7 +183,7 @@ zpass_tc(const TileDesc* __restrict__ tiles, const int2* __restrict__ items, con
     __syncthreads();
     float2* c2 = oth;
     float2* o2 = cur;
-    z_inv_stages<TZ, 1, kZThreads>(count, tw, g, c2, o2);
+    z_inv_stages<TZ, 1, kZThreads>(count, tw, PencilEffectiveStore{g.p, plane, t.hz, t.hz + t.ez}, c2, o2);
   }
   tc::fence_before_sync();
   __syncthreads();
