@@ -795,7 +795,7 @@ void dev_mask(float* psi, const float* const* views, int nviews, long long n, cu
 __global__ void quotient_kernel(float* b, const float* img, long long n) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
     const float x = img[i];
-    b[i] = x > 0.f ? __fdiv_rn(x, b[i]) : 1.f;
+    b[i] = EpiQuotient::quotient(x, b[i]);
   }
 }
 void dev_quotient(float* b, const float* img, long long n, cudaStream_t s) {

@@ -202,7 +202,7 @@ struct EpiQuotient {
   }
   __device__ __forceinline__ void acc_init() {}
   __device__ __forceinline__ static float quotient(float i, float blurred) {
-    return i > 0.f ? __fdiv_rn(i, blurred) : 1.f;
+    return i > 0.f ? __fdividef(i, blurred) : 1.f;  // within 2 ulp (blurred below 2^126)
   }
   __device__ __forceinline__ void operator()(long long g, float blurred) { q[g] = quotient(__ldg(img + g), blurred); }
   template <int K>
@@ -235,8 +235,12 @@ struct StatArchive {
 
 // MVDeconvolution.computeFinalValues / computeNextValue / tikhonov (:603-726).  The reference
 // evaluates tikhonov in double and rounds to float; here the algebraically equal form
-// 2v / (sqrt(1 + 2 lambda v) + 1) is evaluated in float (no cancellation, within a few ulp).
-// Statistics (sum and max of |change|) are accumulated in FP64.
+// 2v / (sqrt(1 + 2 lambda v) + 1) is evaluated in float (no cancellation), its square root as
+// x rsqrt(x) with x = 1 + 2 lambda v >= 1 and its division by the reciprocal intrinsic: within a
+// few ulp.  At the overflow ends the result matches the IEEE form's: an infinite 2v stays
+// infinite, and an infinite x gives NaN where the IEEE form gives 2v / inf = 0, both of which
+// the clamp below turns into minValue.  Statistics (sum and max of |change|) are accumulated
+// in FP64.
 struct EpiUpdate {
   float* psi;
   const float* weight;
@@ -261,8 +265,9 @@ struct EpiUpdate {
     float adjusted;
     if (value > 0.f) {
       if (lambda > 0.f && !isinf(value)) {
-        const float r = __fsqrt_rn(__fadd_rn(1.f, __fmul_rn(2.f * lambda, value)));
-        adjusted = __fdiv_rn(__fmul_rn(2.f, value), __fadd_rn(r, 1.f));
+        const float x = __fadd_rn(1.f, __fmul_rn(2.f * lambda, value));
+        const float r = __fmul_rn(x, rsqrtf(x));
+        adjusted = __fdividef(__fmul_rn(2.f, value), __fadd_rn(r, 1.f));
       } else {
         adjusted = value;
       }
