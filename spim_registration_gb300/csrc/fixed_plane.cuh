@@ -59,6 +59,12 @@ __host__ __device__ constexpr SplitC split_of(int n) {
   return best;
 }
 
+// Voxels per lane of one step of the inverse passes' epilogue walk (a warp per effective row):
+// enough for a whole row of a TX-wide tile, so that a row of, say, 130 voxels takes one step
+// instead of a 128-voxel step and a 2-voxel one.
+template <int TX>
+constexpr int kEpiPerLane = (TX + 31) / 32;
+
 // Shared-memory accessor with compile-time strides: element (batch, i) at
 // p[batch * BS + s(i) * ES], s(i) = i or the skewed i + i/16.
 template <int ES, int BS, bool SKEW>
@@ -266,18 +272,19 @@ plane_inv_fixed(const TileDesc* __restrict__ tiles, const int2* __restrict__ ite
   for (int row = threadIdx.x >> 5; row < t.ey; row += T / 32) {
     const long long g0 = (gz * epi.ny + (t.oy + t.hy + row)) * (long long)epi.nx + t.ox + t.hx;
     const float* src = f + row * (2 * PITCH);
-    for (int x0 = 0; x0 < t.ex; x0 += 128) {
-      int off[4];
-      float val[4];
-      bool ok[4];
+    constexpr int U = kEpiPerLane<TX>;  // one step covers any effective row (ex <= TX)
+    for (int x0 = 0; x0 < t.ex; x0 += 32 * U) {
+      int off[U];
+      float val[U];
+      bool ok[U];
 #pragma unroll
-      for (int u = 0; u < 4; ++u) {
+      for (int u = 0; u < U; ++u) {
         const int x = x0 + lane + 32 * u;
         off[u] = x;
         ok[u] = x < t.ex;
         val[u] = ok[u] ? src[x] : 0.f;
       }
-      epi.template apply<4>(g0, off, val, ok);
+      epi.template apply<U>(g0, off, val, ok);
     }
   }
   epi.finish();

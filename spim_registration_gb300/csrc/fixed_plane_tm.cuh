@@ -301,18 +301,19 @@ plane_inv_tm(const TileDesc* __restrict__ tiles, const int2* __restrict__ items,
   for (int row = threadIdx.x >> 5; row < t.ey; row += T / 32) {
     const long long g0 = (gz * epi.ny + (t.oy + t.hy + row)) * (long long)epi.nx + t.ox + t.hx;
     const float* srow = f + row * (2 * PITCH);
-    for (int x0 = 0; x0 < t.ex; x0 += 128) {
-      int off[4];
-      float val[4];
-      bool ok[4];
+    constexpr int U = kEpiPerLane<TX>;  // one step covers any effective row (ex <= TX)
+    for (int x0 = 0; x0 < t.ex; x0 += 32 * U) {
+      int off[U];
+      float val[U];
+      bool ok[U];
 #pragma unroll
-      for (int u = 0; u < 4; ++u) {
+      for (int u = 0; u < U; ++u) {
         const int x = x0 + lane + 32 * u;
         off[u] = x;
         ok[u] = x < t.ex;
         val[u] = ok[u] ? srow[x] : 0.f;
       }
-      epi.template apply<4>(g0, off, val, ok);
+      epi.template apply<U>(g0, off, val, ok);
     }
   }
   epi.finish();
