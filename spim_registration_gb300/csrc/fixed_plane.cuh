@@ -415,7 +415,8 @@ struct ZRowsLoad {
 // are bit-identical to its output; the halo slices (outside [hz, hz + ez)), which the inverse
 // plane pass never reads, are not stored.
 //
-// The host runs it with 32 pencils per CTA (kZWideChunk), 256 threads and two CTAs per SM:
+// The host runs it with 32 pencils per CTA (kZWideChunk), 256 or 320 threads (zpass_ip_threads)
+// and two CTAs per SM:
 // the one buffer (TZ x 33 complex, 84 KB for 320) takes what two 16-pencil buffers took, and
 // each z slice of a chunk is one 256-byte row in HBM instead of 128 bytes.  On the 512x512x256
 // workload the z pass took 2.79 ms per iteration against 3.36 ms for the two-buffer kernel.  16
@@ -465,6 +466,11 @@ zpass_ip(const TileDesc* __restrict__ tiles, const int2* __restrict__ items, con
   stage_c<R0, TZ, R1, true, false, T>(count, tw, ZRowsLoad<PITCH>{sm},
                                       PencilEffectiveStore{g.p, plane, t.hz, t.hz + t.ez});
 }
+
+// CTA size of the in-place z pass: 320 threads for the 320 / 288 pencils (their middle stage's
+// 640 / 576 butterflies of a 32-pencil chunk take two rounds instead of three; z pass 2.68 vs
+// 2.72 ms per iteration on the 512x512x256 workload, 384 threads 2.89), else 256.
+__host__ __device__ constexpr int zpass_ip_threads(int TZ) { return (TZ == 320 || TZ == 288) ? 320 : kZThreads; }
 
 // Pencil lengths with compiled z-pass kernels: the 4-view 256x256x192 workload's (240, 216)
 // and the 512x512x256 workload's (320, 288).

@@ -39,11 +39,12 @@ static bool launch_z_fixed(PlanTable& pt, const ConvPlan& p, float2* spec, const
 #define MVD_Z_CASE(TZ)                                                                                       \
   if (tz == TZ) {                                                                                            \
     if (z_in_place()) {                                                                                      \
-      auto k = zpass_ip<TZ, kZWideChunk, kZThreads, 2>;                                                      \
+      constexpr int NT = zpass_ip_threads(TZ);                                                               \
+      auto k = zpass_ip<TZ, kZWideChunk, NT, 2>;                                                             \
       const size_t sm = (size_t)TZ * (kZWideChunk + 1) * sizeof(float2);                                     \
       set_smem(k, sm);                                                                                       \
-      k<<<(int)p.items_zw.size(), kZThreads, sm, s>>>(p.d_tiles.as<TileDesc>(), p.d_items_zw.as<int2>(),    \
-                                                      pt.device(), spec, otf);                              \
+      k<<<(int)p.items_zw.size(), NT, sm, s>>>(p.d_tiles.as<TileDesc>(), p.d_items_zw.as<int2>(),           \
+                                               pt.device(), spec, otf);                                     \
       return true;                                                                                           \
     }                                                                                                        \
     auto k = zpass_fixed<TZ, zpass_fixed_occ(TZ)>;                                                         \
