@@ -197,7 +197,8 @@ __device__ __forceinline__ void to_stages(int count, const float2* __restrict__ 
 // ~100 KB per buffer run 512-thread CTAs, two per SM; larger planes run one 1024-thread CTA per
 // SM, so that twice as many warps hide the latency of the gathers and the exchanges (on the
 // 512x512x256 workload 1024 threads measured 23.5 G voxel-updates/s, 768 threads 23.0, 512
-// threads 21.3).
+// threads 21.3).  The in-place kernels of those shapes (fixed_plane_tm.cuh) keep one buffer and
+// run two 512-thread CTAs per SM instead.
 __host__ __device__ constexpr int fixed_ctas_per_sm(int TX, int TY) {
   return 2 * (2 * TY * row_pitch(TX / 2) * 8) <= 227 * 1024 ? 2 : 1;
 }
@@ -483,7 +484,8 @@ __host__ __device__ constexpr int zpass_ip_threads(int TZ) { return (TZ == 320 |
 // Tile shapes (x length, y length, CTA size) with compiled kernels.  They replace the default
 // 384-thread generic kernels: a plan whose CTA size is the default runs them at their own size.
 // 100x100 and 128x100: the 256x256x192 workload's planes (two CTAs per SM); 160x160, 192x96 and
-// 192x135: the 512x512x256 workload's (one CTA per SM).
+// 192x135: the 512x512x256 workload's (one 1024-thread CTA per SM with two buffers; by default
+// these shapes run the in-place kernels of fixed_plane_tm.cuh, two 512-thread CTAs per SM).
 #define MVD_FIXED_PLANE_SHAPES(X) \
   X(100, 100, 512)                \
   X(128, 100, 512)                \
