@@ -194,6 +194,35 @@ def bytes_per_iteration(dec, n_views, n_voxels):
     return out
 
 
+def reference_block_bytes(prob, block):
+    """Algorithmic HBM bytes of one iteration per pass kind under the reference's block
+    structure, the roofline's byte contract: per view, blocks of image + kernel - 1 (one block,
+    MVDeconFFT.java:144-165) or of the given block size (BlockGeneratorFixedSizePrecise.java:
+    46-122, count ceil(n / (B - k + 1)) per axis), P = the block's voxels, H = (X / 2 + 1) Y Z.
+    Per block and convolution: the forward pass reads 4 P and writes 8 H, the z pass reads and
+    writes 8 H each, the inverse pass reads 8 H; the epilogues move 8 (quotient) and 12 (update)
+    bytes per voxel of the volume.  Padding of the tiles this library runs is not credited."""
+    nx, ny, nz = prob.dims_xyz
+    n = nx * ny * nz
+    out = {"plane_fwd": 0, "zpass": 0, "plane_inv_quotient": 0, "plane_inv_update": 0}
+    for psf in prob.psfs:
+        kz, ky, kx = psf.shape
+        if block is None:
+            dims, count = (nx + kx - 1, ny + ky - 1, nz + kz - 1), 1
+        else:
+            dims = tuple(block)
+            count = 1
+            for nd, kd, bd in zip((nx, ny, nz), (kx, ky, kz), block):
+                count *= -(-nd // (bd - kd + 1))
+        P = dims[0] * dims[1] * dims[2]
+        H = (dims[0] // 2 + 1) * dims[1] * dims[2]
+        out["plane_fwd"] += 2 * count * (4 * P + 8 * H)
+        out["zpass"] += 2 * count * 16 * H
+        out["plane_inv_quotient"] += count * 8 * H + 8 * n
+        out["plane_inv_update"] += count * 8 * H + 12 * n
+    return out
+
+
 def max_over_ranks(ms: float, world: int) -> float:
     """Slowest rank's timed region (ms); every rank gets the same value."""
     if world <= 1:
@@ -333,13 +362,17 @@ def run_ours(args, rank, world, local):
 
     # per-pass device time (CUDA events on the library's stream) for the roofline
     prof = dec.profile_iteration()
-    algo = bytes_per_iteration(dec, V, n_vox)
+    algo = reference_block_bytes(prob, WORKLOADS[args.workload][3])  # the byte contract
+    tile = bytes_per_iteration(dec, V, n_vox)  # bytes of the tiles actually transformed
     dom = max(("plane_fwd", "zpass", "plane_inv_quotient", "plane_inv_update"), key=lambda k: prof[k][0])
     dom_ms, dom_launches = prof[dom]
     achieved = algo[dom] / (dom_ms / 1e3) / 1e9
     per_pass = {k: {"ms": round(prof[k][0], 4), "launches": prof[k][1],
-                    "gbs": round(algo[k] / (prof[k][0] / 1e3) / 1e9, 1) if k in algo and prof[k][0] > 0 else None}
+                    "gbs": round(algo[k] / (prof[k][0] / 1e3) / 1e9, 1) if k in algo and prof[k][0] > 0 else None,
+                    "gbs_tile_bytes": round(tile[k] / (prof[k][0] / 1e3) / 1e9, 1)
+                    if k in tile and prof[k][0] > 0 else None}
                 for k in prof}
+    iter_bytes = sum(algo.values())
     traffic = None
     tpath = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(tpath):
@@ -374,7 +407,14 @@ def run_ours(args, rank, world, local):
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                      "frac": achieved / hbm_peak, "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)",
                      "algorithmic_bytes_per_launch": algo[dom] / max(dom_launches, 1),
-                     "avg_launch_ms": dom_ms / max(dom_launches, 1), "traffic": traffic},
+                     "bytes_model": "the reference's block structure (one block of image + kernel - 1 per view, "
+                                    "or the workload's block size): forward pass 4 P + 8 H per block and "
+                                    "convolution; the padding of this library's tiles is not credited",
+                     "avg_launch_ms": dom_ms / max(dom_launches, 1), "traffic": traffic,
+                     "tile_bytes_per_launch": tile[dom] / max(dom_launches, 1),
+                     "frac_with_tile_bytes": tile[dom] / (dom_ms / 1e3) / 1e9 / hbm_peak,
+                     "iteration": {"bytes": iter_bytes, "achieved": iter_bytes / (ms_per_step / 1e3) / 1e9,
+                                   "frac": iter_bytes / (ms_per_step / 1e3) / 1e9 / hbm_peak}},
     }
     if args.tensor_dft:
         out["config"]["flags"] += ", middle DFT stages of the 320 / 288 z passes on the tensor cores"
